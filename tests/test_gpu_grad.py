@@ -1,0 +1,103 @@
+"""Hand-written adjoint against the oracle's forward-mode duals (the stand-in
+for ForwardDiff over the reference's logpdf) and against central differences
+of the GPU forward.  Tolerance: 1e-8 relative (absolute for entries near 0)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import read
+
+pytestmark = pytest.mark.gpu
+GREL = 1e-8
+
+
+def _close(g, ref, rel=GREL):
+    g, ref = np.asarray(g), np.asarray(ref)
+    scale = np.maximum(np.abs(ref), 1.0)
+    return np.max(np.abs(g - ref) / scale)
+
+
+def test_gradient_golden_setting_critical_rates(W, O, ex1_tree, ex1_files):
+    # test/runtests.jl:36-38: x = [ones(n); ones(n); [0.1, 0.2]; 0.8] -- λ = μ
+    # everywhere, so every branch takes the critical formula of getα
+    t = W.readnw(ex1_tree)
+    x = np.r_[np.ones(17), np.ones(17), [0.1, 0.2], 0.8]
+    wm = W.WhaleModel(W.DLWGD(λ=x[:17], μ=x[17:34], q=x[34:36], η=x[36]), t, 0.05)
+    ccds = W.read_ale(os.path.dirname(ex1_files[0]), wm)
+    g = W.gradient(wm, ccds)
+    om = O.OracleModel(ex1_tree, 0.05)
+    otot, og = om.gradient(O.read_ale_files(om, ex1_files), x[:17], x[17:34], q=x[34:36], eta=x[36])
+    assert np.all(np.isfinite(g))
+    assert _close(g, og) <= GREL
+
+
+def test_gradient_general_rates(W, O, ex1_tree, ex1_files):
+    t = W.readnw(ex1_tree)
+    rng = np.random.default_rng(1)
+    lam, mu = rng.normal(-0.5, 0.5, 17), rng.normal(-0.7, 0.5, 17)
+    wm = W.WhaleModel(W.DLWGD(λ=lam, μ=mu, q=[0.3, 0.45], η=0.7), t, 0.05)
+    ccds = W.read_ale(os.path.dirname(ex1_files[0]), wm)
+    tot, gd = W.logpdf_gradient(wm, ccds)
+    g = np.concatenate([gd["λ"], gd["μ"], gd["q"], [gd["η"]]])
+    om = O.OracleModel(ex1_tree, 0.05)
+    otot, og = om.gradient(O.read_ale_files(om, ex1_files), lam, mu, q=[0.3, 0.45], eta=0.7)
+    assert tot == pytest.approx(otot, rel=1e-10)
+    assert _close(g, og) <= GREL
+
+
+def test_gradient_constant_rates(W, O, ex1_tree, ex1_files):
+    t = W.readnw(ex1_tree)
+    wm = W.WhaleModel(W.ConstantDLWGD(λ=0.25, μ=0.35, q=[0.3, 0.45], η=0.7), t, 0.05)
+    ccds = W.read_ale(os.path.dirname(ex1_files[0]), wm)
+    g = W.gradient(wm, ccds)
+    om = O.OracleModel(ex1_tree, 0.05)
+    otot, og = om.gradient(O.read_ale_files(om, ex1_files), [0.25], [0.35], q=[0.3, 0.45], eta=0.7,
+                           kind="ConstantDLWGD")
+    assert _close(g, og) <= GREL
+
+
+def test_gradient_config1_subset(W, O):
+    from whale_gb300 import synth
+
+    wl = synth.config1(n_families=120)
+    wm = wl.model
+    ccds = wl.ccds()
+    keep = [i for i, c in enumerate(ccds) if c.n_clades <= 400][:60]
+    ccds = [ccds[i] for i in keep]
+    g = W.gradient(wm, ccds)
+    om = O.OracleModel(W.nwstr(wm.tree), wm.Δt)
+    occ = [O.OracleCCD(om, wl.ale[i]) for i in keep]
+    r = wm.rates
+    otot, og = om.gradient(occ, r.λ, r.μ, q=r.q, eta=r.η)
+    assert _close(g, og) <= GREL
+
+
+def test_gradient_vs_central_differences_of_gpu_forward(W, O):
+    from whale_gb300 import synth
+
+    wl = synth.config0(seed=5, n_families=30)
+    wm = wl.model
+    ccds = wl.ccds()
+    g = W.gradient(wm, ccds)
+    r = wm.rates
+    base = np.r_[r.λ, r.μ, r.q, r.η]
+    h = 1e-6
+    fd = np.zeros_like(base)
+    for i in range(base.size):
+        xp, xm = base.copy(), base.copy()
+        xp[i] += h
+        xm[i] -= h
+        fp = W.logpdf(wm(W.ConstantDLWGD(λ=xp[0], μ=xp[1], q=xp[2:-1], η=xp[-1])), ccds)
+        fm = W.logpdf(wm(W.ConstantDLWGD(λ=xm[0], μ=xm[1], q=xm[2:-1], η=xm[-1])), ccds)
+        fd[i] = (fp - fm) / (2 * h)
+    assert np.allclose(g, fd, rtol=1e-5, atol=1e-5)
+
+
+def test_gradient_deterministic(W, ex1_tree, ex1_files):
+    t = W.readnw(ex1_tree)
+    wm = W.WhaleModel(W.DLWGD(λ=np.ones(17) * 0.3, μ=np.ones(17) * 0.1, q=[0.2, 0.1], η=0.9), t, 0.05)
+    ccds = W.read_ale(os.path.dirname(ex1_files[0]), wm)
+    a = W.gradient(wm, ccds)
+    b = W.gradient(wm, ccds)
+    assert np.array_equal(a, b)

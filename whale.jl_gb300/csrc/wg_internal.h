@@ -1,0 +1,191 @@
+// Internal declarations shared by the host C++ and the CUDA translation units
+// of libwhalegpu.  Nothing here is part of the public ABI (include/whalegpu.h).
+#pragma once
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/whalegpu.h"
+
+namespace wg {
+
+// Error carried to the C ABI as (status, message).
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string& msg);
+
+// ---------------------------------------------------------------------------
+// Species-tree model: the node order, per-node slice shapes and species sets
+// of a WhaleModel, and the current slice tables [ε, ϕ, ψ] (src/model.jl).
+// ---------------------------------------------------------------------------
+struct Model {
+  int K = 0;                         // nodes, in the reference order
+  std::vector<int> kind, ch0, ch1;   // WG_NODE_*, children (order positions)
+  std::vector<int> nrow, row_off;    // rows per node, prefix offsets (size K+1)
+  std::vector<double> slice_len, leaf_p;
+  int n_words = 0;                   // species bitset words
+  std::vector<uint64_t> clade_bits;  // K * n_words
+  int cond = WG_COND_ROOT;
+  // parameters of the current evaluation
+  bool has_params = false;
+  bool from_rates = false;           // tables were derived from rates (gradient maps back to rates)
+  std::vector<double> lam, mu, q, p; // per node (natural scale)
+  double eta = 0.66;
+  std::vector<double> eps, phi, psi; // per row, sum(nrow)
+  uint64_t version = 0;              // bumped on every parameter change
+  int total_rows() const { return row_off.empty() ? 0 : row_off[K]; }
+  double eps_top(int k) const { return eps[row_off[k] + nrow[k] - 1]; }
+};
+
+// Slice tables from rates (setmodel!, src/model.jl:162-191).
+void model_fill_tables(Model& m);
+// Condition value (src/condition.jl:11-29).
+double model_condition(const Model& m);
+// Adjoint of the condition w.r.t. the tables: adds -scale * d cond to the
+// adjoints of the top ε of the root's children / root and to d_eta.
+void model_condition_vjp(const Model& m, double scale, std::vector<double>& d_eps, double& d_eta);
+// Adjoint of setmodel!: given adjoints of every table entry (eps/phi/psi per
+// row) and of q per node, accumulates adjoints of lam, mu, q, p per node.
+void model_tables_vjp(const Model& m, std::vector<double> d_eps, const std::vector<double>& d_phi,
+                      const std::vector<double>& d_psi, std::vector<double>& d_lam,
+                      std::vector<double>& d_mu, std::vector<double>& d_q, std::vector<double>& d_p);
+
+// ---------------------------------------------------------------------------
+// Conditional clade distribution in the reference layout (src/ccd.jl:80-121):
+// clades ordered by (size, ALE set id), leaves first, ubiquitous clade last.
+// ---------------------------------------------------------------------------
+struct CCD {
+  int n_clades = 0;
+  int64_t observations = 0;
+  int n_genes = 0;
+  std::vector<int> nleaves;
+  std::vector<int64_t> counts;
+  std::vector<int> sp_off, sp;           // species ids per clade (CSR)
+  std::vector<int> split_off, g1, g2;    // splits per clade (CSR), 0-based clade ids
+  std::vector<double> p;                 // Dip / Bip
+};
+
+CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& names,
+               const std::vector<int>& ids);
+
+// ---------------------------------------------------------------------------
+// Packed device layout.  Families are packed into groups; one CTA evaluates
+// one group as a block-diagonal union of its families' CCDs.  For every
+// (group, node) the host emits statically scheduled "sum programs": lane t
+// of the CTA executes entries [j * nt + t], j < J, each accumulating
+// p * A[a] * B[b] into a running sum that is flushed to a partial slot at a
+// segment end.  A finalize pass then combines the partial slots of each clade.
+// ---------------------------------------------------------------------------
+constexpr int kNT = 128;           // threads per CTA of the batched kernels
+constexpr uint64_t kValid = 1;     // entry flags (bits 48..63 of code)
+constexpr uint64_t kEnd = 2;
+
+struct alignas(16) DEntry {
+  uint64_t code;  // a | b << 16 | dst << 32 | flags << 48
+  double p;
+};
+
+struct DProg {
+  int64_t off = 0;  // first entry
+  int32_t J = 0;    // iterations
+  int32_t nt = 0;   // lanes (multiple of 32, <= kNT)
+};
+
+struct DNode {
+  int32_t width = 0;     // row width R (sum of compatible clades over the group's families)
+  int32_t nslot_dup = 0;
+  int64_t top_off = 0;   // doubles: top row in the tops buffer
+  int64_t tab_off = -1;  // doubles: row 0 of this node's table (-1: tables not kept)
+  DProg dup;             // duplication sum over the previous row (also WGD row 1)
+  int64_t fin_dup = 0;   // int2 per clade: (slot start, n segments) of dup
+  DProg r1;              // speciation sum over the children's top rows
+  int64_t fin_r1 = 0;    // int2 per clade for r1
+  int64_t aux = 0;       // int2 per clade: loss map (pos in child0, pos in child1) or leaf flag
+  // adjoint programs (transposed), see the adjoint kernel
+  DProg tdup;            // per clade x: sum over (parent γ, sibling) of p * bar[γ] * row[sib]
+  int64_t fin_tdup = 0;
+  DProg tr1a;            // per clade of child0: sum over entries of p * bar[γ] * top1[sib]
+  int64_t fin_tr1a = 0;
+  DProg tr1b;            // per clade of child1
+  int64_t fin_tr1b = 0;
+  int64_t inv_a = 0;     // int per child0 clade: position in this row (loss term), -1 if none
+  int64_t inv_b = 0;     // int per child1 clade
+  // root only: clade-size levels of the same-row recursion (Πroot)
+  int32_t nlvl = 0;
+  int32_t _pad = 0;
+  int64_t lvl = 0;       // first DLevel
+  int64_t fin_lvl = 0;   // int2 per clade (slots inside its level's program)
+  int64_t lvl_clades = 0;  // ints: clade positions sorted by level
+  int64_t tlvl = 0;        // first DLevel of the transposed level programs (adjoint)
+  int64_t fin_tlvl = 0;
+};
+
+struct DLevel {
+  DProg prog;
+  int32_t begin = 0, end = 0;  // range in lvl_clades
+};
+
+struct DGroup {
+  int32_t n_fam = 0;
+  int32_t maxw = 0;       // max row width over nodes
+  int32_t maxslot = 0;    // max partial slots over programs
+  int32_t _pad = 0;
+  int64_t node0 = 0;      // first DNode (K per group)
+  int64_t fam0 = 0;       // first entry of fam_idx / fam_pos
+  double work = 0;        // estimated DP work (for ordering)
+};
+
+struct Packed {
+  std::vector<DGroup> groups;
+  std::vector<DNode> nodes;
+  std::vector<DEntry> entries;
+  std::vector<int32_t> meta;   // int2 arrays are stored as pairs of int32
+  std::vector<DLevel> levels;
+  std::vector<int32_t> fam_idx, fam_pos;
+  // per original family f and node k (index f * K + k): first DNode of the
+  // family's group, column offset of the family in the group row, columns
+  std::vector<int64_t> fam_node0;
+  std::vector<int32_t> fam_col, fam_ncol;
+  int64_t tops_doubles = 0;
+  int64_t tab_doubles = 0;
+  int32_t max_smem_doubles = 0;
+  double flops_fwd = 0, bytes_fwd = 0, flops_adj = 0;
+};
+
+struct PackOptions {
+  int64_t group_width = 1024;   // target sum of clade counts per group
+  int64_t group_cap = 4096;     // hard cap on the row width of a group
+  bool keep_tables = false;     // allocate table space (adjoint / logpdf!)
+  bool adjoint = false;         // build transposed programs
+  bool single = false;          // one family per group (plain path)
+};
+
+Packed pack_batch(const Model& m, const std::vector<const CCD*>& ccds, const PackOptions& opt);
+
+}  // namespace wg
+
+// Public opaque handles are the internal types.
+struct wg_model : wg::Model {};
+struct wg_ccd : wg::CCD {};
+
+// Run `body`, mapping exceptions to (status, wg_last_error()).
+#define WG_GUARD(...)                                           \
+  try {                                                         \
+    __VA_ARGS__;                                                \
+    return WG_OK;                                               \
+  } catch (const wg::Error& e) {                                \
+    wg::set_last_error(e.what());                               \
+    return e.code;                                              \
+  } catch (const std::bad_alloc&) {                             \
+    wg::set_last_error("host allocation failed");              \
+    return WG_ENOMEM;                                           \
+  } catch (const std::exception& e) {                           \
+    wg::set_last_error(e.what());                               \
+    return WG_EINVAL;                                           \
+  }
+

@@ -1,0 +1,503 @@
+// Packer: turns a batch of CCDs plus the species-tree model into the device
+// layout of the batched DP.
+//
+// What the reference does per call (src/core.jl:41, src/ccd.jl:59-75): for
+// every species node e it lists the clades compatible with e (species(γ) ⊆
+// clade(e), src/ccd.jl:39) in clade-id order and indexes every operand of the
+// DP through index[γ, e] (getl, src/ccd.jl:41-49).  Here that indirection is
+// resolved once, on the host, at batch creation:
+//
+//   * families are packed into groups; a group's row for node e is the
+//     concatenation of its families' compatible-clade lists, so one CTA runs
+//     the DP of all of them in lock step (they share the slice tables);
+//   * every sum over split triples of the DP (Πduplication :178-185,
+//     Πspeciation :160-170, Πwgdretention :187-194, Πroot :151-158) becomes a
+//     statically scheduled "sum program" whose operands are row positions,
+//     so the device never looks anything up;
+//   * speciation terms that are zero in the reference because an operand
+//     clade is incompatible with a child (getl returns 0) are dropped;
+//   * the root's same-row dependency (Πroot reads row 1 of the root itself)
+//     is ordered into levels of the split DAG.
+// The transposed programs the adjoint needs are built here as well.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <numeric>
+
+#include "wg_internal.h"
+
+namespace wg {
+
+namespace {
+
+struct Ent {
+  int a, b;
+  double p;
+};
+
+using Work = std::vector<std::pair<int, std::vector<Ent>>>;  // (destination position, entries)
+
+struct Fin {
+  std::vector<std::array<int, 2>> v;  // per position: slot start, segments
+};
+
+// Statically schedule a sum program.  Lanes get contiguous runs of whole
+// segments (first-fit decreasing into equal-capacity lanes); a clade's
+// entries are split into ceil(s / J) segments so that no lane holds more
+// than J entries.  Cost model: J * warps warp-iterations of FP64 work.
+DProg schedule(const Work& work, std::vector<DEntry>& out, Fin& fin, int& nslots) {
+  DProg prog;
+  prog.off = (int64_t)out.size();
+  int64_t W = 0;
+  for (auto& w : work) W += (int64_t)w.second.size();
+  nslots = 0;
+  if (W == 0) return prog;
+  int best_w = 1;
+  int64_t best_cost = INT64_MAX;
+  for (int w = 1; w <= kNT / 32; ++w) {
+    const int64_t J = (W + 32 * w - 1) / (32 * w);
+    const int64_t cost = J * w;
+    if (cost < best_cost) { best_cost = cost; best_w = w; }
+  }
+  const int NB = 32 * best_w;
+  int J = (int)((W + NB - 1) / NB);
+  struct Seg { int item, k, begin, len; };
+  std::vector<Seg> segs;
+  std::vector<std::vector<int>> bins;
+  while (true) {
+    segs.clear();
+    for (int it = 0; it < (int)work.size(); ++it) {
+      const int s = (int)work[it].second.size();
+      if (s == 0) continue;
+      const int nseg = (s + J - 1) / J;
+      const int base = s / nseg, rem = s % nseg;
+      int start = 0;
+      for (int k = 0; k < nseg; ++k) {
+        const int len = base + (k < rem ? 1 : 0);
+        segs.push_back({it, k, start, len});
+        start += len;
+      }
+    }
+    std::vector<int> order(segs.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return segs[x].len > segs[y].len; });
+    bins.assign(NB, {});
+    std::vector<int> load(NB, 0);
+    bool ok = true;
+    int first_open = 0;
+    for (int si : order) {
+      const int len = segs[si].len;
+      int b = first_open;
+      while (b < NB && load[b] + len > J) ++b;
+      if (b == NB) { ok = false; break; }
+      bins[b].push_back(si);
+      load[b] += len;
+      while (first_open < NB && load[first_open] == J) ++first_open;
+    }
+    if (ok) break;
+    ++J;
+  }
+  // slots: contiguous per destination
+  std::vector<int> slot_start(work.size(), 0);
+  for (int it = 0; it < (int)work.size(); ++it) {
+    const int s = (int)work[it].second.size();
+    if (s == 0) continue;
+    const int nseg = (s + J - 1) / J;
+    slot_start[it] = nslots;
+    fin.v[work[it].first] = {nslots, nseg};
+    nslots += nseg;
+  }
+  if (nslots >= 65535) throw Error(WG_ERANGE, "sum program exceeds 65535 partial slots");
+  int used = 0;
+  for (int b = 0; b < NB; ++b) if (!bins[b].empty()) used = b + 1;
+  const int nt = ((used + 31) / 32) * 32;
+  prog.J = J;
+  prog.nt = nt;
+  out.resize(out.size() + (size_t)J * nt, DEntry{0, 0.0});
+  DEntry* base = out.data() + prog.off;
+  for (int t = 0; t < nt; ++t) {
+    int j = 0;
+    for (int si : bins[t]) {
+      const Seg& sg = segs[si];
+      const auto& ents = work[sg.item].second;
+      const int slot = slot_start[sg.item] + sg.k;
+      for (int q = 0; q < sg.len; ++q, ++j) {
+        const Ent& e = ents[sg.begin + q];
+        const uint64_t flags = kValid | (q == sg.len - 1 ? kEnd : 0);
+        base[(size_t)j * nt + t].code = (uint64_t)e.a | ((uint64_t)e.b << 16) | ((uint64_t)slot << 32) | (flags << 48);
+        base[(size_t)j * nt + t].p = e.p;
+      }
+    }
+  }
+  return prog;
+}
+
+int64_t put_fin(std::vector<int32_t>& meta, const Fin& fin) {
+  if (meta.size() & 1) meta.push_back(0);
+  const int64_t off = (int64_t)meta.size() / 2;  // in int2 units
+  for (auto& f : fin.v) { meta.push_back(f[0]); meta.push_back(f[1]); }
+  return off;
+}
+
+int64_t put_int2(std::vector<int32_t>& meta, const std::vector<std::array<int, 2>>& v) {
+  if (meta.size() & 1) meta.push_back(0);
+  const int64_t off = (int64_t)meta.size() / 2;
+  for (auto& f : v) { meta.push_back(f[0]); meta.push_back(f[1]); }
+  return off;
+}
+
+int64_t put_int(std::vector<int32_t>& meta, const std::vector<int>& v) {
+  const int64_t off = (int64_t)meta.size();
+  meta.insert(meta.end(), v.begin(), v.end());
+  return off;
+}
+
+// Per-family compatibility of clades with species nodes (src/ccd.jl:39,59-75).
+struct FamInfo {
+  std::vector<std::vector<int>> idx;  // [node][clade] -> local column, -1 if incompatible
+  std::vector<int> ncompat;           // [node]
+};
+
+void compat_of(const Model& m, const CCD& c, FamInfo& fi, bool want_idx) {
+  const int W = m.n_words;
+  std::vector<uint64_t> bits((size_t)c.n_clades * W, 0);
+  for (int g = 0; g < c.n_clades; ++g)
+    for (int s = c.sp_off[g]; s < c.sp_off[g + 1]; ++s) {
+      const int id = c.sp[s];
+      if (id < 0 || id >= 64 * W) throw Error(WG_EINVAL, "CCD species id outside the model's species range");
+      bits[(size_t)g * W + (id >> 6)] |= 1ull << (id & 63);
+    }
+  fi.ncompat.assign(m.K, 0);
+  if (want_idx) fi.idx.assign(m.K, std::vector<int>(c.n_clades, -1));
+  for (int k = 0; k < m.K; ++k) {
+    const uint64_t* cl = &m.clade_bits[(size_t)k * W];
+    int n = 0;
+    for (int g = 0; g < c.n_clades; ++g) {
+      const uint64_t* b = &bits[(size_t)g * W];
+      bool ok = true;
+      for (int w = 0; w < W && ok; ++w) ok = (b[w] & ~cl[w]) == 0;
+      if (ok) { if (want_idx) fi.idx[k][g] = n; ++n; }
+    }
+    fi.ncompat[k] = n;
+  }
+}
+
+// Algorithmic FP64 work and bytes of one family, counted on the reference's
+// data structures (every split of every compatible non-leaf clade).
+void family_cost(const Model& m, const CCD& c, const FamInfo& fi, double& flops, double& bytes, double& flops_adj,
+                 double& work) {
+  flops = bytes = flops_adj = work = 0;
+  for (int k = 0; k < m.K; ++k) {
+    double T = 0, Cn = 0, Cnl = 0;
+    for (int g = 0; g < c.n_clades; ++g) {
+      if (fi.idx[k][g] < 0) continue;
+      Cn += 1;
+      if (c.nleaves[g] > 1) { Cnl += 1; T += c.split_off[g + 1] - c.split_off[g]; }
+    }
+    const double n = m.kind[k] == WG_NODE_ROOT ? 0 : m.nrow[k] - 1;
+    flops += n * (3 * T + 2 * Cn + 2 * Cnl);
+    flops_adj += n * (6 * T + 7 * Cn);
+    if (m.kind[k] == WG_NODE_ROOT) { flops += 10 * T + 7 * Cn; flops_adj += 16 * T + 10 * Cn; }
+    else if (m.kind[k] != WG_NODE_LEAF) { flops += 5 * T + 4 * Cn; flops_adj += 8 * T + 6 * Cn; }
+    bytes += 16 * T + 8 * Cn;
+    work += (n + 1) * (T + Cn);
+  }
+  bytes += 8.0 * 3 * m.total_rows() / 1.0 + 8;
+}
+
+// Levels of the split DAG of the root row: a clade's level is one more than
+// the largest level of its split operands; clades without splits are level 0.
+std::vector<int> split_levels(const CCD& c) {
+  std::vector<int> lvl(c.n_clades, 0);
+  for (int g = 0; g < c.n_clades; ++g) {
+    int L = 0;
+    for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s) L = std::max(L, 1 + std::max(lvl[c.g1[s]], lvl[c.g2[s]]));
+    lvl[g] = L;
+  }
+  return lvl;
+}
+
+}  // namespace
+
+Packed pack_batch(const Model& m, const std::vector<const CCD*>& ccds, const PackOptions& opt) {
+  Packed P;
+  const int K = m.K;
+  const int NF = (int)ccds.size();
+  if (NF == 0) throw Error(WG_EINVAL, "empty batch");
+  // ---- pass 1: sizes and work per family
+  std::vector<double> work(NF), width(NF);
+  for (int f = 0; f < NF; ++f) {
+    FamInfo fi;
+    compat_of(m, *ccds[f], fi, true);
+    double fl, by, fa, w;
+    family_cost(m, *ccds[f], fi, fl, by, fa, w);
+    P.flops_fwd += fl;
+    P.bytes_fwd += by;
+    P.flops_adj += fa;
+    work[f] = w;
+    width[f] = ccds[f]->n_clades;
+    if (ccds[f]->n_clades >= 65535) throw Error(WG_ERANGE, "CCD with 65535 or more clades");
+  }
+  // ---- grouping: families sorted by clade count, consecutive ones packed
+  std::vector<int> ord(NF);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return width[a] > width[b]; });
+  std::vector<std::vector<int>> groups;
+  {
+    std::vector<int> cur;
+    int64_t w = 0;
+    for (int f : ord) {
+      if (!cur.empty() && (opt.single || w + (int64_t)width[f] > opt.group_cap || w >= opt.group_width)) {
+        groups.push_back(cur);
+        cur.clear();
+        w = 0;
+      }
+      cur.push_back(f);
+      w += (int64_t)width[f];
+    }
+    if (!cur.empty()) groups.push_back(cur);
+  }
+  // heaviest groups first (they start first on the device)
+  std::vector<double> gwork(groups.size(), 0);
+  for (size_t g = 0; g < groups.size(); ++g)
+    for (int f : groups[g]) gwork[g] += work[f];
+  std::vector<int> gord(groups.size());
+  std::iota(gord.begin(), gord.end(), 0);
+  std::stable_sort(gord.begin(), gord.end(), [&](int a, int b) { return gwork[a] > gwork[b]; });
+
+  int max_smem = 0;
+  P.fam_node0.assign(NF, 0);
+  P.fam_col.assign((size_t)NF * K, 0);
+  P.fam_ncol.assign((size_t)NF * K, 0);
+  for (int gi : gord) {
+    const auto& fams = groups[gi];
+    const int nf = (int)fams.size();
+    std::vector<FamInfo> info(nf);
+    std::vector<std::vector<int>> lvl(nf);
+    for (int i = 0; i < nf; ++i) {
+      compat_of(m, *ccds[fams[i]], info[i], true);
+      lvl[i] = split_levels(*ccds[fams[i]]);
+    }
+    // row offsets of each family in each node's row
+    std::vector<std::vector<int>> off(K, std::vector<int>(nf + 1, 0));
+    std::vector<int> R(K, 0);
+    for (int k = 0; k < K; ++k) {
+      for (int i = 0; i < nf; ++i) off[k][i + 1] = off[k][i] + info[i].ncompat[k];
+      R[k] = off[k][nf];
+      if (R[k] >= 65535) throw Error(WG_ERANGE, "group row wider than 65535 clades");
+    }
+    auto pos = [&](int i, int k, int g) -> int {
+      const int j = info[i].idx[k][g];
+      return j < 0 ? -1 : off[k][i] + j;
+    };
+    DGroup G;
+    G.n_fam = nf;
+    G.node0 = (int64_t)P.nodes.size();
+    G.fam0 = (int64_t)P.fam_idx.size();
+    G.work = gwork[gi];
+    int maxw = 0, maxslot = 0;
+    for (int k = 0; k < K; ++k) maxw = std::max(maxw, R[k]);
+    const int r = K - 1;
+    for (int i = 0; i < nf; ++i) {
+      const CCD& c = *ccds[fams[i]];
+      P.fam_node0[fams[i]] = G.node0;
+      for (int k = 0; k < K; ++k) {
+        P.fam_col[(size_t)fams[i] * K + k] = off[k][i];
+        P.fam_ncol[(size_t)fams[i] * K + k] = info[i].ncompat[k];
+      }
+      P.fam_idx.push_back(fams[i]);
+      P.fam_pos.push_back(pos(i, r, c.n_clades - 1));
+    }
+    for (int k = 0; k < K; ++k) {
+      DNode nd;
+      nd.width = R[k];
+      nd.top_off = P.tops_doubles;
+      P.tops_doubles += R[k];
+      if (opt.keep_tables) {
+        nd.tab_off = P.tab_doubles;
+        P.tab_doubles += (int64_t)m.nrow[k] * R[k];
+      }
+      const int kind = m.kind[k];
+      // ---- duplication program (rows 2.., and WGD row 1)
+      const bool need_dup = (kind != WG_NODE_ROOT) && (m.nrow[k] > 1 || kind == WG_NODE_WGD);
+      if (need_dup) {
+        Work w;
+        Work tw;
+        std::vector<std::vector<Ent>> tby(opt.adjoint ? R[k] : 0);
+        for (int i = 0; i < nf; ++i) {
+          const CCD& c = *ccds[fams[i]];
+          for (int g = 0; g < c.n_clades; ++g) {
+            const int pg = pos(i, k, g);
+            if (pg < 0 || c.nleaves[g] <= 1) continue;
+            std::vector<Ent> es;
+            for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s) {
+              const int a = pos(i, k, c.g1[s]), b = pos(i, k, c.g2[s]);
+              if (a < 0 || b < 0) throw Error(WG_EPARSE, "split operand incompatible with a compatible parent clade");
+              es.push_back({a, b, c.p[s]});
+              if (opt.adjoint) {
+                tby[a].push_back({pg, b, c.p[s]});
+                tby[b].push_back({pg, a, c.p[s]});
+              }
+            }
+            w.emplace_back(pg, std::move(es));
+          }
+        }
+        Fin fin;
+        fin.v.assign(R[k], {0, 0});
+        int ns = 0;
+        nd.dup = schedule(w, P.entries, fin, ns);
+        nd.nslot_dup = ns;
+        maxslot = std::max(maxslot, ns);
+        nd.fin_dup = put_fin(P.meta, fin);
+        if (opt.adjoint) {
+          for (int x = 0; x < R[k]; ++x) if (!tby[x].empty()) tw.emplace_back(x, std::move(tby[x]));
+          Fin tf;
+          tf.v.assign(R[k], {0, 0});
+          nd.tdup = schedule(tw, P.entries, tf, ns);
+          maxslot = std::max(maxslot, ns);
+          nd.fin_tdup = put_fin(P.meta, tf);
+        }
+      }
+      if (kind == WG_NODE_LEAF) {
+        std::vector<std::array<int, 2>> aux(R[k], {0, 0});
+        for (int i = 0; i < nf; ++i) {
+          const CCD& c = *ccds[fams[i]];
+          for (int g = 0; g < c.n_clades; ++g) {
+            const int pg = pos(i, k, g);
+            if (pg >= 0 && c.nleaves[g] == 1) aux[pg] = {1, 0};
+          }
+        }
+        nd.aux = put_int2(P.meta, aux);
+      }
+      if (kind == WG_NODE_WGD) {
+        if (R[k] != R[m.ch0[k]]) throw Error(WG_EINVAL, "WGD node and its child differ in compatible clades");
+      }
+      if (kind == WG_NODE_INTERNAL || kind == WG_NODE_ROOT) {
+        const int ka = m.ch0[k], kb = m.ch1[k];
+        Work w;
+        std::vector<std::array<int, 2>> aux(R[k], {-1, -1});
+        std::vector<std::vector<Ent>> ta(opt.adjoint ? R[ka] : 0), tb(opt.adjoint ? R[kb] : 0);
+        std::vector<int> inva(R[ka], -1), invb(R[kb], -1);
+        for (int i = 0; i < nf; ++i) {
+          const CCD& c = *ccds[fams[i]];
+          for (int g = 0; g < c.n_clades; ++g) {
+            const int pg = pos(i, k, g);
+            if (pg < 0) continue;
+            const int la = pos(i, ka, g), lb = pos(i, kb, g);
+            aux[pg] = {la, lb};
+            if (la >= 0) inva[la] = pg;
+            if (lb >= 0) invb[lb] = pg;
+            if (c.nleaves[g] <= 1) continue;
+            std::vector<Ent> es;
+            for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s) {
+              const int g1 = c.g1[s], g2 = c.g2[s];
+              const int a1 = pos(i, ka, g1), b2 = pos(i, kb, g2);
+              const int b1 = pos(i, kb, g1), a2 = pos(i, ka, g2);
+              if (a1 >= 0 && b2 >= 0) {
+                es.push_back({a1, b2, c.p[s]});
+                if (opt.adjoint) { ta[a1].push_back({pg, b2, c.p[s]}); tb[b2].push_back({pg, a1, c.p[s]}); }
+              }
+              if (b1 >= 0 && a2 >= 0) {
+                es.push_back({a2, b1, c.p[s]});
+                if (opt.adjoint) { ta[a2].push_back({pg, b1, c.p[s]}); tb[b1].push_back({pg, a2, c.p[s]}); }
+              }
+            }
+            if (!es.empty()) w.emplace_back(pg, std::move(es));
+          }
+        }
+        Fin fin;
+        fin.v.assign(R[k], {0, 0});
+        int ns = 0;
+        nd.r1 = schedule(w, P.entries, fin, ns);
+        maxslot = std::max(maxslot, ns);
+        nd.fin_r1 = put_fin(P.meta, fin);
+        nd.aux = put_int2(P.meta, aux);
+        if (opt.adjoint) {
+          Work wa, wb;
+          for (int x = 0; x < R[ka]; ++x) if (!ta[x].empty()) wa.emplace_back(x, std::move(ta[x]));
+          for (int x = 0; x < R[kb]; ++x) if (!tb[x].empty()) wb.emplace_back(x, std::move(tb[x]));
+          Fin fa, fb;
+          fa.v.assign(R[ka], {0, 0});
+          fb.v.assign(R[kb], {0, 0});
+          nd.tr1a = schedule(wa, P.entries, fa, ns);
+          maxslot = std::max(maxslot, ns);
+          nd.fin_tr1a = put_fin(P.meta, fa);
+          nd.tr1b = schedule(wb, P.entries, fb, ns);
+          maxslot = std::max(maxslot, ns);
+          nd.fin_tr1b = put_fin(P.meta, fb);
+          nd.inv_a = put_int(P.meta, inva);
+          nd.inv_b = put_int(P.meta, invb);
+        }
+      }
+      if (kind == WG_NODE_ROOT) {
+        int nl = 0;
+        for (int i = 0; i < nf; ++i)
+          for (int v : lvl[i]) nl = std::max(nl, v + 1);
+        std::vector<Work> lw(nl), tlw(nl);
+        std::vector<std::vector<int>> lc(nl);
+        std::vector<std::vector<Ent>> tby(opt.adjoint ? R[k] : 0);
+        std::vector<int> plevel(R[k], 0);
+        for (int i = 0; i < nf; ++i) {
+          const CCD& c = *ccds[fams[i]];
+          for (int g = 0; g < c.n_clades; ++g) {
+            const int pg = pos(i, k, g);
+            plevel[pg] = lvl[i][g];
+            lc[lvl[i][g]].push_back(pg);
+            if (c.nleaves[g] <= 1) continue;
+            std::vector<Ent> es;
+            for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s) {
+              const int a = pos(i, k, c.g1[s]), b = pos(i, k, c.g2[s]);
+              es.push_back({a, b, c.p[s]});
+              if (opt.adjoint) { tby[a].push_back({pg, b, c.p[s]}); tby[b].push_back({pg, a, c.p[s]}); }
+            }
+            lw[lvl[i][g]].emplace_back(pg, std::move(es));
+          }
+        }
+        if (opt.adjoint)
+          for (int x = 0; x < R[k]; ++x) if (!tby[x].empty()) tlw[plevel[x]].emplace_back(x, std::move(tby[x]));
+        Fin fin, tfin;
+        fin.v.assign(R[k], {0, 0});
+        tfin.v.assign(R[k], {0, 0});
+        std::vector<int> lcl;
+        nd.nlvl = nl;
+        nd.lvl = (int64_t)P.levels.size();
+        for (int L = 0; L < nl; ++L) {
+          DLevel dl;
+          int ns = 0;
+          dl.prog = schedule(lw[L], P.entries, fin, ns);
+          maxslot = std::max(maxslot, ns);
+          dl.begin = (int)lcl.size();
+          lcl.insert(lcl.end(), lc[L].begin(), lc[L].end());
+          dl.end = (int)lcl.size();
+          P.levels.push_back(dl);
+        }
+        nd.fin_lvl = put_fin(P.meta, fin);
+        nd.lvl_clades = put_int(P.meta, lcl);
+        if (opt.adjoint) {
+          nd.tlvl = (int64_t)P.levels.size();
+          for (int L = 0; L < nl; ++L) {
+            DLevel dl;
+            int ns = 0;
+            dl.prog = schedule(tlw[L], P.entries, tfin, ns);
+            maxslot = std::max(maxslot, ns);
+            dl.begin = P.levels[nd.lvl + L].begin;
+            dl.end = P.levels[nd.lvl + L].end;
+            P.levels.push_back(dl);
+          }
+          nd.fin_tlvl = put_fin(P.meta, tfin);
+        }
+      }
+      P.nodes.push_back(nd);
+    }
+    G.maxw = maxw;
+    G.maxslot = maxslot;
+    // shared memory: cur, nxt/X, Y, slots (+ adjoint: one more row)
+    const int smem = (opt.adjoint ? 5 : 3) * maxw + maxslot + 8;
+    max_smem = std::max(max_smem, smem);
+    P.groups.push_back(G);
+  }
+  P.max_smem_doubles = max_smem;
+  return P;
+}
+
+}  // namespace wg
