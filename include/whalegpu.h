@@ -127,15 +127,16 @@ int wg_ccd_export(const wg_ccd* c, int32_t* nleaves, int64_t* counts, int32_t* s
 int wg_batch_create(wg_ctx* ctx, const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_t flags,
                     wg_batch** out);
 int wg_batch_destroy(wg_batch* b);
-/* n_groups: CTAs of the batched launch; device_bytes: device memory held;
+/* n_groups: tasks (CTAs over all launches); device_bytes: device memory held;
  * flops_fwd / bytes_fwd: algorithmic FP64 flops and bytes of one forward
  * (counted from the packed layout). */
 int wg_batch_info(const wg_batch* b, int32_t* n_families, int32_t* n_groups, int64_t* device_bytes,
                   double* flops_fwd, double* bytes_fwd, double* flops_adj);
 
 /* Pack a batch on the host only (no device needed) and report its layout:
- * groups (CTAs), sum-program entries, DP-table doubles kept for the adjoint,
- * shared memory per CTA (bytes) and the algorithmic forward FLOPs. */
+ * tasks (CTAs over all launches), program entries, DP-table doubles kept for
+ * the adjoint, largest shared memory per CTA (bytes) and the algorithmic
+ * forward FLOPs. */
 int wg_pack_info(const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_t flags, int64_t* n_groups,
                  int64_t* n_entries, int64_t* table_doubles, int64_t* smem_bytes, double* flops_fwd);
 

@@ -219,14 +219,14 @@ int wg_pack_info(const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_
   WG_GUARD({
     if (!m || !ccds || n_ccds <= 0) throw wg::Error(WG_EINVAL, "wg_pack_info: bad arguments");
     std::vector<const wg::CCD*> cs(ccds, ccds + n_ccds);
-    wg::PackOptions opt;
+    wg::PackOptions2 opt;
     opt.adjoint = (flags & WG_BATCH_GRAD) != 0;
     opt.keep_tables = (flags & (WG_BATCH_GRAD | WG_BATCH_TABLES)) != 0;
-    wg::Packed P = wg::pack_batch(*m, cs, opt);
-    if (n_groups) *n_groups = (int64_t)P.groups.size();
+    wg::Packed2 P = wg::pack_batch2(*m, cs, opt);
+    if (n_groups) *n_groups = (int64_t)P.tasks.size();
     if (n_entries) *n_entries = (int64_t)P.entries.size();
     if (table_doubles) *table_doubles = P.tab_doubles;
-    if (smem_bytes) *smem_bytes = (int64_t)P.max_smem_doubles * 8;
+    if (smem_bytes) *smem_bytes = (int64_t)P.max_smem * 8;
     if (flops_fwd) *flops_fwd = P.flops_fwd;
   });
 }

@@ -167,6 +167,94 @@ struct PackOptions {
 
 Packed pack_batch(const Model& m, const std::vector<const CCD*>& ccds, const PackOptions& opt);
 
+// ---------------------------------------------------------------------------
+// Batched layout (level-synchronous tasks).  A task is one species node for a
+// group of families; the tasks of one height level of the species tree are
+// independent and run in one launch, one CTA per task.  Every task runs
+// host-scheduled lane programs whose entries are either products
+// (acc += p * A[a] * B[b]) or finalize ops that consume acc and write a row
+// value; clades too long for one lane are split into partial slots that a
+// short combine pass (after one barrier) finishes.
+// ---------------------------------------------------------------------------
+namespace op {
+enum : uint32_t {
+  PROD = 0,
+  FIN_DUP = 1,     // out[c] = ψ·acc + ϕ·in[c]
+  FIN_SPEC = 2,    // out[c] = acc + (A[a]·εb + B[b]·εa)
+  FIN_WGD = 3,     // out[c] = q·acc + ((1-q)·A[a] + 2qεf·A[a])
+  FIN_LVL = 4,     // cur[c] = ca·acc + cb·cur[c]            (root, in place)
+  FIN_PART = 5,    // part[slot] = acc
+  FIN_ADJ = 6,     // barn[c] = ψ·acc + ϕ·bar[c]; dϕ += bar[c]·L[c]; dψ += acc·L[c]
+  FIN_TOP = 7,     // bartop[c] = acc + (bar[a]·ε)             (speciation/loss adjoint)
+  FIN_WGDADJ = 8,  // bartop[c] = ((1-q) + 2qεf)·bar[c] + q·acc; dq, dεf
+  FIN_TLVL = 9,    // bar[c] += ca·acc; dca += acc·L[c]/2     (root levels, reverse)
+  NOP = 15,
+};
+}
+
+struct DProg2 {
+  int64_t off = 0;      // entries [j * nt + lane]
+  int32_t J = 0;
+  int32_t nt = 0;       // lanes used (multiple of 32)
+  int64_t comb = 0;     // combine entries (one per split clade)
+  int32_t ncomb = 0;
+  int32_t nslot = 0;
+};
+
+struct DTask {
+  int32_t node = 0;     // model order position
+  int32_t width = 0;    // R: row width (sum of compatible clades of its families)
+  int32_t wa = 0, wb = 0;  // staged widths of child 0 / child 1 top rows
+  int32_t nfam = 0;     // families (root tasks: log L outputs)
+  int32_t smem = 0;     // shared doubles needed
+  int64_t tab = -1;     // DP table base, task-major [row][R] (-1: not kept)
+  int64_t top = 0;      // top row base in the tops buffer
+  int64_t gmap = 0;     // int64 per staged position (wa + wb): offset in tops
+  int64_t aux = 0;      // leaf tasks: int per clade, 1 for leaf clades
+  int64_t loss = 0;     // int2 per clade: positions in stage A / stage B (-1)
+  int64_t inva = 0;     // int per stage-A position: row position of that clade (-1)
+  int64_t invb = 0;     // int per stage-B position
+  DProg2 dup, init;     // forward: rows >= 1, row 0
+  DProg2 tdup;          // adjoint of rows >= 1 (and WGD row 0)
+  DProg2 ta, tb;        // adjoint of the speciation row 0, per child
+  int32_t nlvl = 0;     // root: levels of the same-row recursion
+  int32_t _pad = 0;
+  int64_t lvl = 0;      // first DProg2 of the level programs (forward)
+  int64_t tlvl = 0;     // first DProg2 of the level programs (adjoint)
+  int64_t fam = 0;      // root: int2 per family (family index, ubiquitous position)
+  int64_t gout = 0;     // adjoint: per-task outputs, 2 * nrow + 5 doubles
+};
+
+struct Packed2 {
+  std::vector<DTask> tasks;
+  std::vector<DEntry> entries;
+  std::vector<int32_t> meta;
+  std::vector<int64_t> gmap;
+  std::vector<DProg2> progs;               // level programs
+  std::vector<std::vector<int32_t>> levels;  // task indices per launch level
+  std::vector<int32_t> level_smem;         // max shared doubles per level (forward)
+  std::vector<int32_t> level_smem_adj;     // max shared doubles per level (adjoint)
+  int64_t tops_doubles = 0, tab_doubles = 0, gout_doubles = 0;
+  // gradient reduction: for every output j (3 NR + K + 1), the gout indices
+  // that contribute, in a fixed order (CSR)
+  std::vector<int64_t> red_off, red_idx;
+  // per family f and node k (f * K + k): table base, row width, column, columns
+  std::vector<int64_t> fam_tab;
+  std::vector<int32_t> fam_w, fam_col, fam_ncol;
+  double flops_fwd = 0, bytes_fwd = 0, flops_adj = 0;
+  int32_t max_smem = 0;
+};
+
+struct PackOptions2 {
+  int64_t target_ops = 768;   // product + finalize ops per row per task
+  int64_t max_width = 6144;   // cap on a task's row width
+  bool keep_tables = false;
+  bool adjoint = false;
+  int nt = 128;               // threads per CTA
+};
+
+Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const PackOptions2& opt);
+
 }  // namespace wg
 
 // Public opaque handles are the internal types.

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstring>
 #include <numeric>
 
 #include "wg_internal.h"
@@ -497,6 +498,470 @@ Packed pack_batch(const Model& m, const std::vector<const CCD*>& ccds, const Pac
     P.groups.push_back(G);
   }
   P.max_smem_doubles = max_smem;
+  return P;
+}
+
+}  // namespace wg
+
+// ===========================================================================
+// Batched layout: level-synchronous (node, family group) tasks
+// ===========================================================================
+namespace wg {
+
+namespace {
+
+struct Item {
+  int c = 0;                  // output position of the finalize op
+  uint32_t fin = op::FIN_DUP;
+  int fa = 0xFFFF, fb = 0xFFFF;
+  std::vector<Ent> prods;
+};
+
+inline uint64_t pack_code(uint32_t f0, uint32_t f1, uint32_t f2, uint32_t opc) {
+  return (uint64_t)(f0 & 0xFFFFu) | ((uint64_t)(f1 & 0xFFFFu) << 16) | ((uint64_t)(f2 & 0xFFFFu) << 32) |
+         ((uint64_t)opc << 48);
+}
+
+inline double bits_to_double(uint64_t b) {
+  double d;
+  std::memcpy(&d, &b, sizeof d);
+  return d;
+}
+
+// Lane programs with fused finalize.  An item (one clade) is its products
+// followed by its finalize op; items longer than J ops are split into
+// segments ending in FIN_PART, finished by a combine entry after a barrier.
+DProg2 schedule2(std::vector<Item>& items, int ntmax, std::vector<DEntry>& out) {
+  DProg2 pr;
+  pr.off = (int64_t)out.size();
+  int64_t W = 0;
+  int maxops = 0;
+  for (auto& it : items) {
+    W += (int64_t)it.prods.size() + 1;
+    maxops = std::max(maxops, (int)it.prods.size() + 1);
+  }
+  if (W == 0) return pr;
+  int best_w = 1;
+  int64_t best_cost = INT64_MAX;
+  for (int w = 1; w <= ntmax / 32; ++w) {
+    const int64_t J = (W + 32 * w - 1) / (32 * w);
+    const int64_t cost = J * w;
+    if (cost <= best_cost) { best_cost = cost; best_w = w; }  // ties: more warps, shorter rows
+  }
+  const int NB = 32 * best_w;
+  int J = (int)((W + NB - 1) / NB);
+  struct Seg { int item, k, begin, len; bool split; };
+  std::vector<Seg> segs;
+  std::vector<std::vector<int>> bins;
+  std::vector<int> nseg(items.size(), 1);
+  while (true) {
+    if (maxops > J && J < 2) J = 2;
+    segs.clear();
+    for (int i = 0; i < (int)items.size(); ++i) {
+      const int np = (int)items[i].prods.size();
+      if (np + 1 <= J) {
+        nseg[i] = 1;
+        segs.push_back({i, 0, 0, np, false});
+        continue;
+      }
+      const int per = J - 1;  // products per segment (+ FIN_PART)
+      const int ns = (np + per - 1) / per;
+      nseg[i] = ns;
+      const int base = np / ns, rem = np % ns;
+      int b = 0;
+      for (int k = 0; k < ns; ++k) {
+        const int len = base + (k < rem ? 1 : 0);
+        segs.push_back({i, k, b, len, true});
+        b += len;
+      }
+    }
+    std::vector<int> order(segs.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return segs[x].len > segs[y].len; });
+    bins.assign(NB, {});
+    std::vector<int> load(NB, 0);
+    bool ok = true;
+    int first_open = 0;
+    for (int si : order) {
+      const int len = segs[si].len + 1;
+      int b = first_open;
+      while (b < NB && load[b] + len > J) ++b;
+      if (b == NB) { ok = false; break; }
+      bins[b].push_back(si);
+      load[b] += len;
+      while (first_open < NB && load[first_open] == J) ++first_open;
+    }
+    if (ok) break;
+    ++J;
+  }
+  // partial slots of split items, contiguous per item
+  std::vector<int> slot0(items.size(), -1);
+  int nslot = 0;
+  for (int i = 0; i < (int)items.size(); ++i)
+    if (nseg[i] > 1) { slot0[i] = nslot; nslot += nseg[i]; }
+  if (nslot >= 65535) throw Error(WG_ERANGE, "program exceeds 65535 partial slots");
+  int used = 0;
+  for (int b = 0; b < NB; ++b) if (!bins[b].empty()) used = b + 1;
+  const int nt = ((used + 31) / 32) * 32;
+  pr.J = J;
+  pr.nt = nt;
+  pr.nslot = nslot;
+  out.resize(out.size() + (size_t)J * nt, DEntry{pack_code(0, 0, 0, op::NOP), 0.0});
+  DEntry* base = out.data() + pr.off;
+  for (int t = 0; t < nt; ++t) {
+    int j = 0;
+    for (int si : bins[t]) {
+      const Seg& sg = segs[si];
+      const Item& it = items[sg.item];
+      for (int q = 0; q < sg.len; ++q, ++j) {
+        const Ent& e = it.prods[sg.begin + q];
+        base[(size_t)j * nt + t] = DEntry{pack_code(e.a, e.b, 0, op::PROD), e.p};
+      }
+      if (sg.split)
+        base[(size_t)j * nt + t] = DEntry{pack_code(0, 0, slot0[sg.item] + sg.k, op::FIN_PART), 0.0};
+      else
+        base[(size_t)j * nt + t] = DEntry{pack_code(it.c, it.fa, it.fb, it.fin), 0.0};
+      ++j;
+    }
+  }
+  // combine entries
+  pr.comb = (int64_t)out.size();
+  for (int i = 0; i < (int)items.size(); ++i) {
+    if (nseg[i] <= 1) continue;
+    const uint64_t sl = (uint64_t)(uint32_t)slot0[i] | ((uint64_t)(uint32_t)nseg[i] << 32);
+    out.push_back(DEntry{pack_code(items[i].c, items[i].fa, items[i].fb, items[i].fin), bits_to_double(sl)});
+    ++pr.ncomb;
+  }
+  return pr;
+}
+
+}  // namespace
+
+Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const PackOptions2& opt) {
+  Packed2 P;
+  const int K = m.K;
+  const int NF = (int)ccds.size();
+  if (NF == 0) throw Error(WG_EINVAL, "empty batch");
+  const int NR = m.total_rows();
+  // ---- per family: compatibility, levels, cost
+  std::vector<FamInfo> info(NF);
+  std::vector<std::vector<int>> lvl(NF);
+  for (int f = 0; f < NF; ++f) {
+    if (ccds[f]->n_clades >= 65535) throw Error(WG_ERANGE, "CCD with 65535 or more clades");
+    compat_of(m, *ccds[f], info[f], true);
+    double fl, by, fa, w;
+    family_cost(m, *ccds[f], info[f], fl, by, fa, w);
+    P.flops_fwd += fl;
+    P.bytes_fwd += by;
+    P.flops_adj += fa;
+    lvl[f] = split_levels(*ccds[f]);
+  }
+  // per (family, node) location of the top row, filled as tasks are built
+  std::vector<int64_t> toploc((size_t)NF * K, -1);
+  P.fam_tab.assign((size_t)NF * K, -1);
+  P.fam_w.assign((size_t)NF * K, 0);
+  P.fam_col.assign((size_t)NF * K, 0);
+  P.fam_ncol.assign((size_t)NF * K, 0);
+  // height levels of the species tree
+  std::vector<int> height(K, 0);
+  int H = 0;
+  for (int k = 0; k < K; ++k) {
+    if (m.ch0[k] >= 0) height[k] = std::max(height[k], height[m.ch0[k]] + 1);
+    if (m.ch1[k] >= 0) height[k] = std::max(height[k], height[m.ch1[k]] + 1);
+    H = std::max(H, height[k]);
+  }
+  P.levels.assign(H + 1, {});
+  P.level_smem.assign(H + 1, 0);
+  P.level_smem_adj.assign(H + 1, 0);
+  // gradient reduction contributions
+  std::vector<std::vector<int64_t>> red(3 * (size_t)NR + K + 1);
+  auto eps_top_row = [&](int k) { return m.row_off[k] + m.nrow[k] - 1; };
+  const int NT = opt.nt;
+
+  for (int k = 0; k < K; ++k) {
+    const int kind = m.kind[k];
+    const int ka = m.ch0[k], kb = m.ch1[k];
+    // families with compatible clades at k, heaviest first
+    std::vector<std::pair<double, int>> fw;
+    for (int f = 0; f < NF; ++f) {
+      const int C = info[f].ncompat[k];
+      if (C == 0) continue;
+      const CCD& c = *ccds[f];
+      double T = 0;
+      for (int g = 0; g < c.n_clades; ++g)
+        if (info[f].idx[k][g] >= 0 && c.nleaves[g] > 1) T += c.split_off[g + 1] - c.split_off[g];
+      fw.emplace_back(T + C, f);
+    }
+    std::stable_sort(fw.begin(), fw.end(), [](auto& x, auto& y) { return x.first > y.first; });
+    // next-fit into tasks
+    std::vector<std::vector<int>> groups;
+    {
+      std::vector<int> cur;
+      double ops = 0;
+      int64_t width = 0;
+      for (auto& [w, f] : fw) {
+        const int C = info[f].ncompat[k];
+        if (!cur.empty() && (ops + w > opt.target_ops || width + C > opt.max_width)) {
+          groups.push_back(cur);
+          cur.clear();
+          ops = 0;
+          width = 0;
+        }
+        cur.push_back(f);
+        ops += w;
+        width += C;
+      }
+      if (!cur.empty()) groups.push_back(cur);
+    }
+    for (auto& fams : groups) {
+      const int nf = (int)fams.size();
+      DTask T;
+      T.node = k;
+      T.nfam = nf;
+      std::vector<int> col(nf + 1, 0), cola(nf + 1, 0), colb(nf + 1, 0);
+      for (int i = 0; i < nf; ++i) {
+        col[i + 1] = col[i] + info[fams[i]].ncompat[k];
+        if (ka >= 0) cola[i + 1] = cola[i] + info[fams[i]].ncompat[ka];
+        if (kb >= 0) colb[i + 1] = colb[i] + info[fams[i]].ncompat[kb];
+      }
+      const int R = col[nf];
+      if (R >= 32768) throw Error(WG_ERANGE, "task row wider than 32767 clades");
+      T.width = R;
+      T.wa = cola[nf];
+      T.wb = colb[nf];
+      auto pos = [&](int i, int g) { const int j = info[fams[i]].idx[k][g]; return j < 0 ? -1 : col[i] + j; };
+      auto posa = [&](int i, int g) { const int j = info[fams[i]].idx[ka][g]; return j < 0 ? -1 : cola[i] + j; };
+      auto posb = [&](int i, int g) { const int j = info[fams[i]].idx[kb][g]; return j < 0 ? -1 : colb[i] + j; };
+      T.top = P.tops_doubles;
+      P.tops_doubles += R;
+      if (opt.keep_tables) {
+        T.tab = P.tab_doubles;
+        P.tab_doubles += (int64_t)m.nrow[k] * R;
+      }
+      for (int i = 0; i < nf; ++i) {
+        const size_t fk = (size_t)fams[i] * K + k;
+        toploc[fk] = T.top + col[i];
+        P.fam_tab[fk] = T.tab;
+        P.fam_w[fk] = R;
+        P.fam_col[fk] = col[i];
+        P.fam_ncol[fk] = info[fams[i]].ncompat[k];
+      }
+      // staging maps of the children's top rows
+      T.gmap = (int64_t)P.gmap.size();
+      for (int ch : {ka, kb}) {
+        if (ch < 0) continue;
+        for (int i = 0; i < nf; ++i) {
+          const int C = info[fams[i]].ncompat[ch];
+          const int64_t src = toploc[(size_t)fams[i] * K + ch];
+          for (int j = 0; j < C; ++j) P.gmap.push_back(src + j);
+        }
+      }
+      // ---- forward programs
+      const bool has_rows = kind != WG_NODE_ROOT && m.nrow[k] > 1;
+      if (has_rows || (opt.adjoint && kind == WG_NODE_WGD)) {
+        std::vector<Item> items, titems;
+        // row programs read both operand fields of every entry: finalize
+        // entries carry their own clade in f0 and f1
+        if (opt.adjoint) {
+          titems.resize(R);
+          for (int x = 0; x < R; ++x) { titems[x].c = x; titems[x].fin = op::FIN_ADJ; titems[x].fa = x; titems[x].fb = x; }
+        }
+        for (int i = 0; i < nf; ++i) {
+          const CCD& c = *ccds[fams[i]];
+          for (int g = 0; g < c.n_clades; ++g) {
+            const int pg = pos(i, g);
+            if (pg < 0) continue;
+            Item it;
+            it.c = pg;
+            it.fin = op::FIN_DUP;
+            it.fa = pg;
+            it.fb = pg;
+            if (c.nleaves[g] > 1)
+              for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s) {
+                const int a = pos(i, c.g1[s]), b = pos(i, c.g2[s]);
+                if (a < 0 || b < 0) throw Error(WG_EPARSE, "split operand incompatible with a compatible clade");
+                it.prods.push_back({a, b, c.p[s]});
+                if (opt.adjoint) {
+                  titems[a].prods.push_back({pg, b, c.p[s]});
+                  titems[b].prods.push_back({pg, a, c.p[s]});
+                }
+              }
+            items.push_back(std::move(it));
+          }
+        }
+        if (has_rows) T.dup = schedule2(items, NT, P.entries);
+        if (opt.adjoint) T.tdup = schedule2(titems, NT, P.entries);
+      }
+      if (kind == WG_NODE_LEAF) {
+        std::vector<int> aux(R, 0);
+        for (int i = 0; i < nf; ++i) {
+          const CCD& c = *ccds[fams[i]];
+          for (int g = 0; g < c.n_clades; ++g) {
+            const int pg = pos(i, g);
+            if (pg >= 0 && c.nleaves[g] == 1) aux[pg] = 1;
+          }
+        }
+        T.aux = put_int(P.meta, aux);
+      } else if (kind == WG_NODE_WGD) {
+        if (T.wa != R) throw Error(WG_EINVAL, "WGD node and its child differ in compatible clades");
+        std::vector<Item> items;
+        for (int i = 0; i < nf; ++i) {
+          const CCD& c = *ccds[fams[i]];
+          for (int g = 0; g < c.n_clades; ++g) {
+            const int pg = pos(i, g);
+            if (pg < 0) continue;
+            Item it;
+            it.c = pg;
+            it.fin = op::FIN_WGD;
+            it.fa = posa(i, g);
+            if (c.nleaves[g] > 1)
+              for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s)
+                it.prods.push_back({posa(i, c.g1[s]), posa(i, c.g2[s]), c.p[s]});
+            items.push_back(std::move(it));
+          }
+        }
+        T.init = schedule2(items, NT, P.entries);
+      } else {
+        // speciation + loss (internal) or Πspec + Πloss of the root row
+        std::vector<Item> items;
+        std::vector<std::array<int, 2>> loss(R, {-1, -1});
+        std::vector<int> inva(T.wa, -1), invb(T.wb, -1);
+        std::vector<Item> ta, tb;
+        if (opt.adjoint) {
+          ta.resize(T.wa);
+          tb.resize(T.wb);
+          for (int x = 0; x < T.wa; ++x) { ta[x].c = x; ta[x].fin = op::FIN_TOP; }
+          for (int x = 0; x < T.wb; ++x) { tb[x].c = x; tb[x].fin = op::FIN_TOP; }
+        }
+        for (int i = 0; i < nf; ++i) {
+          const CCD& c = *ccds[fams[i]];
+          for (int g = 0; g < c.n_clades; ++g) {
+            const int pg = pos(i, g);
+            if (pg < 0) continue;
+            const int la = posa(i, g), lb = posb(i, g);
+            loss[pg] = {la, lb};
+            if (la >= 0) inva[la] = pg;
+            if (lb >= 0) invb[lb] = pg;
+            Item it;
+            it.c = pg;
+            it.fin = op::FIN_SPEC;
+            it.fa = la < 0 ? 0xFFFF : la;
+            it.fb = lb < 0 ? 0xFFFF : lb;
+            if (c.nleaves[g] > 1)
+              for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s) {
+                const int g1 = c.g1[s], g2 = c.g2[s];
+                const int a1 = posa(i, g1), b2 = posb(i, g2), b1 = posb(i, g1), a2 = posa(i, g2);
+                if (a1 >= 0 && b2 >= 0) {
+                  it.prods.push_back({a1, b2, c.p[s]});
+                  if (opt.adjoint) { ta[a1].prods.push_back({pg, b2, c.p[s]}); tb[b2].prods.push_back({pg, a1, c.p[s]}); }
+                }
+                if (b1 >= 0 && a2 >= 0) {
+                  it.prods.push_back({a2, b1, c.p[s]});
+                  if (opt.adjoint) { ta[a2].prods.push_back({pg, b1, c.p[s]}); tb[b1].prods.push_back({pg, a2, c.p[s]}); }
+                }
+              }
+            items.push_back(std::move(it));
+          }
+        }
+        T.init = schedule2(items, NT, P.entries);
+        T.loss = put_int2(P.meta, loss);
+        if (opt.adjoint) {
+          for (int x = 0; x < T.wa; ++x) ta[x].fa = inva[x] < 0 ? 0xFFFF : inva[x];
+          for (int x = 0; x < T.wb; ++x) tb[x].fa = invb[x] < 0 ? 0xFFFF : invb[x];
+          T.ta = schedule2(ta, NT, P.entries);
+          T.tb = schedule2(tb, NT, P.entries);
+          T.inva = put_int(P.meta, inva);
+          T.invb = put_int(P.meta, invb);
+        }
+      }
+      if (kind == WG_NODE_ROOT) {
+        int nl = 0;
+        for (int i = 0; i < nf; ++i)
+          for (int v : lvl[fams[i]]) nl = std::max(nl, v + 1);
+        std::vector<std::vector<Item>> lw(nl), tlw(nl);
+        std::vector<std::vector<int>> lvl_of_pos;
+        std::vector<int> plevel(R, 0);
+        for (int i = 0; i < nf; ++i) {
+          const CCD& c = *ccds[fams[i]];
+          for (int g = 0; g < c.n_clades; ++g) plevel[pos(i, g)] = lvl[fams[i]][g];
+        }
+        std::vector<Item> tby;
+        if (opt.adjoint) { tby.resize(R); for (int x = 0; x < R; ++x) { tby[x].c = x; tby[x].fin = op::FIN_TLVL; } }
+        for (int i = 0; i < nf; ++i) {
+          const CCD& c = *ccds[fams[i]];
+          for (int g = 0; g < c.n_clades; ++g) {
+            const int pg = pos(i, g);
+            Item it;
+            it.c = pg;
+            it.fin = op::FIN_LVL;
+            if (c.nleaves[g] > 1)
+              for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s) {
+                const int a = pos(i, c.g1[s]), b = pos(i, c.g2[s]);
+                it.prods.push_back({a, b, c.p[s]});
+                if (opt.adjoint) { tby[a].prods.push_back({pg, b, c.p[s]}); tby[b].prods.push_back({pg, a, c.p[s]}); }
+              }
+            lw[plevel[pg]].push_back(std::move(it));
+          }
+        }
+        if (opt.adjoint)
+          for (int x = 0; x < R; ++x) tlw[plevel[x]].push_back(std::move(tby[x]));
+        T.nlvl = nl;
+        T.lvl = (int64_t)P.progs.size();
+        for (int L = 0; L < nl; ++L) P.progs.push_back(schedule2(lw[L], NT, P.entries));
+        if (opt.adjoint) {
+          T.tlvl = (int64_t)P.progs.size();
+          for (int L = 0; L < nl; ++L) P.progs.push_back(schedule2(tlw[L], NT, P.entries));
+        }
+        std::vector<std::array<int, 2>> fam(nf);
+        for (int i = 0; i < nf; ++i) fam[i] = {fams[i], pos(i, ccds[fams[i]]->n_clades - 1)};
+        T.fam = put_int2(P.meta, fam);
+      }
+      // shared memory: cur + nxt rows (children staged in nxt) + slots + spare
+      int slots = std::max({T.dup.nslot, T.init.nslot, T.tdup.nslot, T.ta.nslot, T.tb.nslot});
+      for (int64_t q = T.lvl; q < (int64_t)P.progs.size(); ++q) slots = std::max(slots, P.progs[q].nslot);
+      // forward: cur, nxt (children staged in nxt); adjoint: bar, barn, two
+      // L rows, G; then partial slots and reduction scratch
+      const int W2 = std::max(R, T.wa + T.wb);
+      T.smem = 2 * W2 + slots + 16 * (opt.nt / 32) + 32;
+      const int smem_adj = 5 * W2 + slots + 16 * (opt.nt / 32) + 32;
+      if (opt.adjoint) {
+        T.gout = P.gout_doubles;
+        const int n = m.nrow[k];
+        P.gout_doubles += 2 * (int64_t)n + 5;
+        for (int r = 1; r < n && kind != WG_NODE_ROOT; ++r) {
+          red[NR + m.row_off[k] + r].push_back(T.gout + 2 * r);
+          red[2 * (size_t)NR + m.row_off[k] + r].push_back(T.gout + 2 * r + 1);
+        }
+        if (ka >= 0) red[eps_top_row(ka)].push_back(T.gout + 2 * n + 0);
+        if (kb >= 0) red[eps_top_row(kb)].push_back(T.gout + 2 * n + 1);
+        if (kind == WG_NODE_WGD) red[3 * (size_t)NR + k].push_back(T.gout + 2 * n + 2);
+        if (kind == WG_NODE_ROOT) {
+          red[3 * (size_t)NR + K].push_back(T.gout + 2 * n + 3);
+          red[eps_top_row(k)].push_back(T.gout + 2 * n + 4);
+        }
+      }
+      P.levels[height[k]].push_back((int32_t)P.tasks.size());
+      P.level_smem[height[k]] = std::max(P.level_smem[height[k]], T.smem);
+      P.max_smem = std::max(P.max_smem, T.smem);
+      if (opt.adjoint) {
+        P.level_smem_adj[height[k]] = std::max(P.level_smem_adj[height[k]], smem_adj);
+        P.max_smem = std::max(P.max_smem, smem_adj);
+      }
+      P.tasks.push_back(T);
+    }
+  }
+  // heaviest tasks first inside each level
+  for (auto& L : P.levels)
+    std::stable_sort(L.begin(), L.end(), [&](int a, int b) {
+      const DTask& x = P.tasks[a];
+      const DTask& y = P.tasks[b];
+      return (int64_t)x.dup.J * m.nrow[x.node] + x.init.J > (int64_t)y.dup.J * m.nrow[y.node] + y.init.J;
+    });
+  P.red_off.assign(red.size() + 1, 0);
+  for (size_t j = 0; j < red.size(); ++j) {
+    P.red_off[j + 1] = P.red_off[j] + (int64_t)red[j].size();
+    P.red_idx.insert(P.red_idx.end(), red[j].begin(), red[j].end());
+  }
   return P;
 }
 
