@@ -140,6 +140,12 @@ int wg_batch_info(const wg_batch* b, int32_t* n_families, int32_t* n_groups, int
 int wg_pack_info(const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_t flags, int64_t* n_groups,
                  int64_t* n_entries, int64_t* table_doubles, int64_t* smem_bytes, double* flops_fwd);
 
+/* Per-task schedule of the packed layout (tuning aid): 12 ints per task:
+ * node, level, width, families, rows-program J and lanes, row-0 program J and
+ * lanes, adjoint rows-program J and lanes, root levels, shared doubles. */
+int wg_pack_tasks(const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_t flags, int32_t* out,
+                  int64_t cap, int64_t* n_tasks);
+
 /* ---- likelihood -------------------------------------------------------
  * per_family[i] = log L_i (-Inf when L_i <= 0) without conditioning
  * (src/core.jl:39-43); total = sum_i per_family[i] - N * condition, non-finite

@@ -231,4 +231,30 @@ int wg_pack_info(const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_
   });
 }
 
+int wg_pack_tasks(const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_t flags, int32_t* out,
+                  int64_t cap, int64_t* n_tasks) {
+  WG_GUARD({
+    if (!m || !ccds || n_ccds <= 0 || !n_tasks) throw wg::Error(WG_EINVAL, "wg_pack_tasks: bad arguments");
+    std::vector<const wg::CCD*> cs(ccds, ccds + n_ccds);
+    wg::PackOptions2 opt;
+    opt.adjoint = (flags & WG_BATCH_GRAD) != 0;
+    opt.keep_tables = (flags & (WG_BATCH_GRAD | WG_BATCH_TABLES)) != 0;
+    wg::Packed2 P = wg::pack_batch2(*m, cs, opt);
+    *n_tasks = (int64_t)P.tasks.size();
+    if (!out) return WG_OK;
+    std::vector<int> level(P.tasks.size(), 0);
+    for (size_t L = 0; L < P.levels.size(); ++L) {
+      for (int t : P.levels[L]) level[t] = (int)L;
+      for (int t : P.levels_h[L]) level[t] = (int)L;
+    }
+    for (size_t t = 0; t < P.tasks.size() && (int64_t)(t + 1) * 12 <= cap; ++t) {
+      const wg::DTask& T = P.tasks[t];
+      int32_t* o = out + 12 * t;
+      o[0] = T.node; o[1] = level[t]; o[2] = T.width; o[3] = T.nfam;
+      o[4] = T.dup.J; o[5] = T.dup.nt; o[6] = T.init.J; o[7] = T.init.nt;
+      o[8] = T.tdup.J; o[9] = T.tdup.nt; o[10] = T.nlvl; o[11] = T.smem;
+    }
+  });
+}
+
 }  // extern "C"

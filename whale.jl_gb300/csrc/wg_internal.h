@@ -206,7 +206,9 @@ struct DTask {
   int32_t width = 0;    // R: row width (sum of compatible clades of its families)
   int32_t wa = 0, wb = 0;  // staged widths of child 0 / child 1 top rows
   int32_t nfam = 0;     // families (root tasks: log L outputs)
-  int32_t smem = 0;     // shared doubles needed
+  int32_t smem = 0;     // shared doubles needed (forward)
+  int32_t nt = 0;       // threads of the CTA that runs the task
+  int32_t _pad2 = 0;
   int64_t tab = -1;     // DP table base, task-major [row][R] (-1: not kept)
   int64_t top = 0;      // top row base in the tops buffer
   int64_t gmap = 0;     // int64 per staged position (wa + wb): offset in tops
@@ -231,9 +233,10 @@ struct Packed2 {
   std::vector<int32_t> meta;
   std::vector<int64_t> gmap;
   std::vector<DProg2> progs;               // level programs
-  std::vector<std::vector<int32_t>> levels;  // task indices per launch level
-  std::vector<int32_t> level_smem;         // max shared doubles per level (forward)
-  std::vector<int32_t> level_smem_adj;     // max shared doubles per level (adjoint)
+  // task indices per launch level, for light (kNT2L threads) and heavy
+  // (kNT2H threads) tasks, with the largest shared memory of each launch
+  std::vector<std::vector<int32_t>> levels, levels_h;
+  std::vector<int32_t> level_smem, level_smem_adj, level_smem_h, level_smem_adj_h;
   int64_t tops_doubles = 0, tab_doubles = 0, gout_doubles = 0;
   // gradient reduction: for every output j (3 NR + K + 1), the gout indices
   // that contribute, in a fixed order (CSR)
@@ -245,12 +248,16 @@ struct Packed2 {
   int32_t max_smem = 0;
 };
 
+constexpr int kNT2L = 128;   // threads per CTA of light tasks
+constexpr int kNT2H = 256;   // threads per CTA of heavy (single large family) tasks
+
 struct PackOptions2 {
-  int64_t target_ops = 768;   // product + finalize ops per row per task
+  int64_t target_ops = 320;   // forward product + finalize ops per row per task
+  int64_t heavy_ops = 1024;   // non-root tasks above this many ops per row get kNT2H threads
   int64_t max_width = 6144;   // cap on a task's row width
+  int target_j = 3;           // iterations per row the lane scheduler aims for
   bool keep_tables = false;
   bool adjoint = false;
-  int nt = 128;               // threads per CTA
 };
 
 Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const PackOptions2& opt);

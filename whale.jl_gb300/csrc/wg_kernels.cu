@@ -220,7 +220,6 @@ __global__ void __launch_bounds__(256) k_fp64_probe(double* out, int iters, doub
 // Batched kernels: one CTA per (species node, family group) task; the tasks
 // of one height level of the species tree run in one launch.
 // ===========================================================================
-constexpr int kNT2 = 128;  // threads per CTA
 
 struct KArgs2 {
   const DTask* tasks;
@@ -277,16 +276,67 @@ __device__ __forceinline__ void run_any(const DEntry* __restrict__ E, const DPro
 }
 
 // Combine pass for split clades (one thread per clade).
-template <class Fin>
+template <int NT, class Fin>
 __device__ __forceinline__ void run_comb(const DEntry* __restrict__ E, const DProg2& pr, const double* part,
                                          Fin fin) {
-  for (int i = threadIdx.x; i < pr.ncomb; i += kNT2) {
+  for (int i = threadIdx.x; i < pr.ncomb; i += NT) {
     const ulonglong2 raw = __ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + i));
     const Raw x = decode(raw);
     const unsigned s0 = (unsigned)(raw.y & 0xFFFFFFFFu), n = (unsigned)(raw.y >> 32);
     double s = part[s0];
     for (unsigned k = 1; k < n; ++k) s += part[s0 + k];
     fin(x.opc, x.f0, x.f1, x.f2, s);
+  }
+}
+
+// The same-row levels of the root (Πroot): level after level with a barrier
+// between them.  Levels are short, so the next level's descriptor and first
+// entries are loaded before the barrier that ends the current one.
+template <int NT, bool REVERSE = false, class Fin>
+__device__ __forceinline__ void run_levels(const DEntry* __restrict__ E, const DProg2* __restrict__ progs, int nlvl,
+                                           int lane, const double* A, const double* B, double* part, Fin fin) {
+  if (nlvl <= 0) return;
+  auto at = [&](int i) { return REVERSE ? nlvl - 1 - i : i; };
+  DProg2 cur = progs[at(0)];
+  ulonglong2 pre0 = make_ulonglong2(0, (uint64_t)op::NOP << 48), pre1 = pre0;
+  if (lane < cur.nt) {
+    const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + cur.off) + lane;
+    if (cur.J > 0) pre0 = __ldg(e);
+    if (cur.J > 1) pre1 = __ldg(e + cur.nt);
+  }
+  for (int i = 0; i < nlvl; ++i) {
+    DProg2 nxt;
+    if (i + 1 < nlvl) nxt = progs[at(i + 1)];
+    if (lane < cur.nt) {
+      const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + cur.off) + lane;
+      double acc = 0.0;
+      for (int j = 0; j < cur.J; ++j) {
+        const Raw x = decode(j == 0 ? pre0 : (j == 1 ? pre1 : __ldg(e + (size_t)j * cur.nt)));
+        if (x.opc == op::PROD) {
+          acc = fma(x.p * A[x.f0], B[x.f1], acc);
+        } else if (x.opc == op::FIN_PART) {
+          part[x.f2] = acc;
+          acc = 0.0;
+        } else if (x.opc != op::NOP) {
+          fin(x.opc, x.f0, x.f1, x.f2, acc);
+          acc = 0.0;
+        }
+      }
+    }
+    if (cur.ncomb) {
+      __syncthreads();
+      run_comb<NT>(E, cur, part, fin);
+    }
+    if (i + 1 < nlvl) {
+      pre0 = pre1 = make_ulonglong2(0, (uint64_t)op::NOP << 48);
+      if (lane < nxt.nt) {
+        const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + nxt.off) + lane;
+        if (nxt.J > 0) pre0 = __ldg(e);
+        if (nxt.J > 1) pre1 = __ldg(e + nxt.nt);
+      }
+      cur = nxt;
+    }
+    __syncthreads();
   }
 }
 
@@ -323,8 +373,8 @@ __device__ __forceinline__ double eps_top2(const KArgs2& A, int k) {
   return A.params[A.row_off[k] + A.mnode[k].w - 1];
 }
 
-template <bool TABLES>
-__global__ void __launch_bounds__(kNT2) k_fwd2(const KArgs2 A, const int* __restrict__ list) {
+template <bool TABLES, int NT>
+__global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restrict__ list) {
   extern __shared__ double sm[];
   const DTask& T = A.tasks[list[blockIdx.x]];
   const int k = T.node;
@@ -332,7 +382,7 @@ __global__ void __launch_bounds__(kNT2) k_fwd2(const KArgs2 A, const int* __rest
   const int R = T.width;
   const int W2 = max(R, T.wa + T.wb);
   const int tid = threadIdx.x;
-  const int lane = (tid + 32 * (int)(blockIdx.x & 3)) & (kNT2 - 1);
+  const int lane = (tid + 32 * (int)(blockIdx.x & (NT / 32 - 1))) & (NT - 1);
   double* cur = sm;
   double* nxt = sm + W2;
   double* part = sm + 2 * W2;
@@ -342,10 +392,10 @@ __global__ void __launch_bounds__(kNT2) k_fwd2(const KArgs2 A, const int* __rest
   if (mn.x == WG_NODE_LEAF) {
     const int* aux = A.meta + T.aux;
     const double lp = A.leafp[k];
-    for (int c = tid; c < R; c += kNT2) cur[c] = aux[c] ? lp : 0.0;
+    for (int c = tid; c < R; c += NT) cur[c] = aux[c] ? lp : 0.0;
   } else {
     const int64_t* gm = A.gmap + T.gmap;
-    for (int i = tid; i < T.wa + T.wb; i += kNT2) nxt[i] = A.tops[gm[i]];
+    for (int i = tid; i < T.wa + T.wb; i += NT) nxt[i] = A.tops[gm[i]];
     __syncthreads();
     const double* X = nxt;
     const double* Y = nxt + T.wa;
@@ -359,7 +409,7 @@ __global__ void __launch_bounds__(kNT2) k_fwd2(const KArgs2 A, const int* __rest
       run_any(E, T.init, lane, X, X, part, fin);
       if (T.init.ncomb) {
         __syncthreads();
-        run_comb(E, T.init, part, fin);
+        run_comb<NT>(E, T.init, part, fin);
       }
     } else {
       const double ea = eps_top2(A, mn.y), eb = eps_top2(A, mn.z);
@@ -371,7 +421,7 @@ __global__ void __launch_bounds__(kNT2) k_fwd2(const KArgs2 A, const int* __rest
       run_any(E, T.init, lane, X, Y, part, fin);
       if (T.init.ncomb) {
         __syncthreads();
-        run_comb(E, T.init, part, fin);
+        run_comb<NT>(E, T.init, part, fin);
       }
       if (mn.x == WG_NODE_ROOT) {
         // whaleroot! (src/core.jl:130-149), Πroot over smaller clades of the
@@ -383,21 +433,13 @@ __global__ void __launch_bounds__(kNT2) k_fwd2(const KArgs2 A, const int* __rest
         const double ca = (1.0 - eta) * xi / eta;
         const double cb = eta * (1.0 - er) / (xi * xi);
         auto lfin = [&](unsigned, unsigned c, unsigned, unsigned, double acc) { cur[c] = fma(ca, acc, cb * cur[c]); };
-        for (int L = 0; L < T.nlvl; ++L) {
-          const DProg2 lp = A.progs[T.lvl + L];
-          run_any(E, lp, lane, cur, cur, part, lfin);
-          if (lp.ncomb) {
-            __syncthreads();
-            run_comb(E, lp, part, lfin);
-          }
-          __syncthreads();
-        }
+        run_levels<NT>(E, A.progs + T.lvl, T.nlvl, lane, cur, cur, part, lfin);
       }
     }
   }
   __syncthreads();
   if (TABLES)
-    for (int c = tid; c < R; c += kNT2) A.tabs[T.tab + c] = cur[c];
+    for (int c = tid; c < R; c += NT) A.tabs[T.tab + c] = cur[c];
   if (mn.x != WG_NODE_ROOT) {
     for (int r = 1; r < mn.w; ++r) {
       const double ph = A.params[NR + roff + r], ps = A.params[2 * NR + roff + r];
@@ -410,7 +452,7 @@ __global__ void __launch_bounds__(kNT2) k_fwd2(const KArgs2 A, const int* __rest
           nxt[c] = v;
           if (TABLES) tr[c] = v;
         };
-        run_comb(E, T.dup, part, cfin);
+        run_comb<NT>(E, T.dup, part, cfin);
       }
       __syncthreads();
       double* t = cur;
@@ -419,10 +461,10 @@ __global__ void __launch_bounds__(kNT2) k_fwd2(const KArgs2 A, const int* __rest
     }
   }
   double* top = A.tops + T.top;
-  for (int c = tid; c < R; c += kNT2) top[c] = cur[c];
+  for (int c = tid; c < R; c += NT) top[c] = cur[c];
   if (mn.x == WG_NODE_ROOT) {
     const int2* fam = reinterpret_cast<const int2*>(A.meta) + T.fam;
-    for (int f = tid; f < T.nfam; f += kNT2) {
+    for (int f = tid; f < T.nfam; f += NT) {
       const int2 fp = fam[f];
       const double L = cur[fp.y];
       A.logl[fp.x] = L > 0.0 ? log(L) : -INFINITY;
@@ -468,6 +510,7 @@ __device__ __forceinline__ double reduce_scatter16(double (&v)[8], double (&w)[8
   return a[0];
 }
 
+template <int NT>
 __device__ __forceinline__ void block_sum4(double (&v)[4], double* red) {
   for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
@@ -481,7 +524,7 @@ __device__ __forceinline__ void block_sum4(double (&v)[4], double* red) {
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     double s = 0.0;
-    for (int q = 0; q < kNT2 / 32; ++q) s += red[4 * q + i];
+    for (int q = 0; q < NT / 32; ++q) s += red[4 * q + i];
     v[i] = s;
   }
 }
@@ -489,7 +532,8 @@ __device__ __forceinline__ void block_sum4(double (&v)[4], double* red) {
 // Reverse sweep of one task.  Per-task outputs (gout + T.gout):
 // [2r] ∂/∂ϕ_r, [2r+1] ∂/∂ψ_r (rows r >= 1), [2n] ∂/∂ε_top(child 0),
 // [2n+1] ∂/∂ε_top(child 1), [2n+2] ∂/∂q, [2n+3] ∂/∂η, [2n+4] ∂/∂ε_top(own).
-__global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __restrict__ list) {
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == 128 ? 8 : 2) k_adj2(const KArgs2 A, const int* __restrict__ list) {
   extern __shared__ double sm[];
   const DTask& T = A.tasks[list[blockIdx.x]];
   const int k = T.node;
@@ -497,7 +541,7 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
   const int R = T.width;
   const int W2 = max(R, T.wa + T.wb);
   const int tid = threadIdx.x;
-  const int lane = (tid + 32 * (int)(blockIdx.x & 3)) & (kNT2 - 1);
+  const int lane = (tid + 32 * (int)(blockIdx.x & (NT / 32 - 1))) & (NT - 1);
   const int NR = A.NR;
   const int roff = A.row_off[k];
   const int n = mn.w;
@@ -515,13 +559,13 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
   const int64_t* gm = A.gmap + T.gmap;
   if (mn.x == WG_NODE_ROOT) {
     const double* row0 = A.tabs + T.tab;
-    for (int c = tid; c < R; c += kNT2) {
+    for (int c = tid; c < R; c += NT) {
       L0[c] = row0[c];
       bar[c] = 0.0;
     }
     __syncthreads();
     const int2* fam = reinterpret_cast<const int2*>(A.meta) + T.fam;
-    for (int f = tid; f < T.nfam; f += kNT2) {
+    for (int f = tid; f < T.nfam; f += NT) {
       const double L = L0[fam[f].y];
       bar[fam[f].y] = L > 0.0 ? 1.0 / L : 0.0;
     }
@@ -536,19 +580,11 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
       bar[c] += ca * g;
       acc4[0] += 0.5 * g * L0[c];
     };
-    for (int L = T.nlvl - 1; L >= 0; --L) {
-      const DProg2 lp = A.progs[T.tlvl + L];
-      run_any(E, lp, lane, bar, L0, part, tfin);
-      if (lp.ncomb) {
-        __syncthreads();
-        run_comb(E, lp, part, tfin);
-      }
-      __syncthreads();
-    }
+    run_levels<NT, true>(E, A.progs + T.tlvl, T.nlvl, lane, bar, L0, part, tfin);
     // stage the children's tops, recompute Πspec + Πloss for ∂/∂cb
     double* X = barn;
     double* Y = barn + T.wa;
-    for (int i = tid; i < T.wa + T.wb; i += kNT2) barn[i] = A.tops[gm[i]];
+    for (int i = tid; i < T.wa + T.wb; i += NT) barn[i] = A.tops[gm[i]];
     __syncthreads();
     const double ea = eps_top2(A, mn.y), eb = eps_top2(A, mn.z);
     double* bbc = L1;  // cb · bar, the adjoint of Πspec + Πloss
@@ -562,9 +598,9 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
     run_any(E, T.init, lane, X, Y, part, sfin);
     if (T.init.ncomb) {
       __syncthreads();
-      run_comb(E, T.init, part, sfin);
+      run_comb<NT>(E, T.init, part, sfin);
     }
-    for (int c = tid; c < R; c += kNT2) {
+    for (int c = tid; c < R; c += NT) {
       const double b = cb * bar[c];
       bbc[c] = b;
       const int2 l = loss[c];
@@ -578,7 +614,7 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
     run_any(E, T.ta, lane, bbc, Y, part, afin);
     if (T.ta.ncomb) {
       __syncthreads();
-      run_comb(E, T.ta, part, afin);
+      run_comb<NT>(E, T.ta, part, afin);
     }
     __syncthreads();
     auto bfin = [&](unsigned, unsigned x, unsigned fa, unsigned, double acc) {
@@ -587,9 +623,9 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
     run_any(E, T.tb, lane, bbc, X, part, bfin);
     if (T.tb.ncomb) {
       __syncthreads();
-      run_comb(E, T.tb, part, bfin);
+      run_comb<NT>(E, T.tb, part, bfin);
     }
-    block_sum4(acc4, red);
+    block_sum4<NT>(acc4, red);
     if (tid == 0) {
       const double dxi_deta = er, dxi_der = -(1.0 - eta);
       const double dca_deta = (-xi + (1.0 - eta) * dxi_deta) / eta - (1.0 - eta) * xi / (eta * eta);
@@ -605,7 +641,7 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
     return;
   }
   // ---- rows n-1 .. 1 of the branch (within_branch!)
-  for (int c = tid; c < R; c += kNT2) bar[c] = A.bartops[T.top + c];
+  for (int c = tid; c < R; c += NT) bar[c] = A.bartops[T.top + c];
   double rp[8], rs[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) rp[i] = rs[i] = 0.0;
@@ -613,7 +649,7 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
   for (int r = n - 1; r >= 1; --r) {
     double* Lp = ((n - 1 - r) & 1) ? L1 : L0;
     const double* lr = A.tabs + T.tab + (int64_t)(r - 1) * R;
-    for (int c = tid; c < R; c += kNT2) Lp[c] = lr[c];
+    for (int c = tid; c < R; c += NT) Lp[c] = lr[c];
     __syncthreads();
     const double ph = A.params[NR + roff + r], ps = A.params[2 * NR + roff + r];
     // products G[x] = Σ p·bar[γ]·L[sib] and bar_{r-1}[x] = ϕ bar[x] + ψ G[x]
@@ -643,12 +679,12 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
         barn[c] = fma(ps, g, ph * bar[c]);
         Gs[c] = g;
       };
-      run_comb(E, T.tdup, part, cfin);
+      run_comb<NT>(E, T.tdup, part, cfin);
     }
     __syncthreads();
     // ∂/∂ϕ_r = Σ bar_r·L_{r-1}, ∂/∂ψ_r = ½ Σ G·L_{r-1} (each split counted twice)
     double dphi = 0.0, dpsi = 0.0;
-    for (int c = tid; c < R; c += kNT2) {
+    for (int c = tid; c < R; c += NT) {
       const double l = Lp[c];
       dphi = fma(bar[c], l, dphi);
       dpsi = fma(Gs[c], l, dpsi);
@@ -666,7 +702,7 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
       __syncthreads();
       if (tid < 16) {
         double s = 0.0;
-        for (int q = 0; q < kNT2 / 32; ++q) s += red[16 * q + tid];
+        for (int q = 0; q < NT / 32; ++q) s += red[16 * q + tid];
         const int i = tid & 7;
         const int rr = r + slot - i;  // row of batch slot i
         if (i <= slot) out[2 * rr + (tid >> 3)] = (tid >> 3) ? 0.5 * s : s;
@@ -682,7 +718,7 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
   // ---- row 0
   if (mn.x == WG_NODE_WGD) {
     double* X = L0;
-    for (int i = tid; i < T.wa; i += kNT2) X[i] = A.tops[gm[i]];
+    for (int i = tid; i < T.wa; i += NT) X[i] = A.tops[gm[i]];
     __syncthreads();
     const double q = A.params[3 * NR + k];
     const double ef = eps_top2(A, mn.y);
@@ -707,9 +743,9 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
     }
     if (T.tdup.ncomb) {
       __syncthreads();
-      run_comb(E, T.tdup, part, wfin);
+      run_comb<NT>(E, T.tdup, part, wfin);
     }
-    block_sum4(acc4, red);
+    block_sum4<NT>(acc4, red);
     if (tid == 0) {
       out[2 * n + 2] = acc4[0];
       out[2 * n + 0] = acc4[1];
@@ -717,7 +753,7 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
   } else if (mn.x == WG_NODE_INTERNAL) {
     double* X = L0;
     double* Y = L0 + T.wa;
-    for (int i = tid; i < T.wa + T.wb; i += kNT2) L0[i] = A.tops[gm[i]];
+    for (int i = tid; i < T.wa + T.wb; i += NT) L0[i] = A.tops[gm[i]];
     __syncthreads();
     const double ea = eps_top2(A, mn.y), eb = eps_top2(A, mn.z);
     auto afin = [&](unsigned, unsigned x, unsigned fa, unsigned, double acc) {
@@ -726,7 +762,7 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
     run_any(E, T.ta, lane, bar, Y, part, afin);
     if (T.ta.ncomb) {
       __syncthreads();
-      run_comb(E, T.ta, part, afin);
+      run_comb<NT>(E, T.ta, part, afin);
     }
     __syncthreads();
     auto bfin = [&](unsigned, unsigned x, unsigned fa, unsigned, double acc) {
@@ -735,17 +771,17 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
     run_any(E, T.tb, lane, bar, X, part, bfin);
     if (T.tb.ncomb) {
       __syncthreads();
-      run_comb(E, T.tb, part, bfin);
+      run_comb<NT>(E, T.tb, part, bfin);
     }
     double acc4[4] = {0.0, 0.0, 0.0, 0.0};  // dea, deb
     const int2* loss = reinterpret_cast<const int2*>(A.meta) + T.loss;
-    for (int c = tid; c < R; c += kNT2) {
+    for (int c = tid; c < R; c += NT) {
       const int2 l = loss[c];
       const double b = bar[c];
       acc4[0] += b * (l.y >= 0 ? Y[l.y] : 0.0);
       acc4[1] += b * (l.x >= 0 ? X[l.x] : 0.0);
     }
-    block_sum4(acc4, red);
+    block_sum4<NT>(acc4, red);
     if (tid == 0) {
       out[2 * n + 0] = acc4[0];
       out[2 * n + 1] = acc4[1];
@@ -753,14 +789,17 @@ __global__ void __launch_bounds__(kNT2) k_adj2(const KArgs2 A, const int* __rest
   }
 }
 
-// Gradient reduction: out[j] = Σ gout[idx] over the fixed contributor list of j.
+// Gradient reduction: out[j] = Σ gout[idx] over the fixed contributor list of
+// j; one warp per output, lane-strided partial sums and a fixed butterfly.
 __global__ void k_reduce2(const double* __restrict__ gout, const int64_t* __restrict__ off,
                           const int64_t* __restrict__ idx, int P, double* __restrict__ out) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (j >= P) return;
   double s = 0.0;
-  for (int64_t i = off[j]; i < off[j + 1]; ++i) s += gout[idx[i]];
-  out[j] = s;
+  for (int64_t i = off[j] + lane; i < off[j + 1]; i += 32) s += gout[idx[i]];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[j] = s;
 }
 
 // ---------------------------------------------------------------------------
@@ -793,6 +832,8 @@ void h2d(T* d, const std::vector<T>& h, cudaStream_t s) {
 struct wg_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;  // heavy tasks of a level run here, joined back per level
+  cudaEvent_t fork = nullptr, join = nullptr;
   int n_sm = 0;
   size_t smem_optin = 0;
   bool timing = false;
@@ -864,8 +905,8 @@ struct wg_batch {
   uint32_t flags = 0;
   int64_t device_bytes = 0;
   double flops_fwd = 0, bytes_fwd = 0, flops_adj = 0;
-  std::vector<int> lvl_off, lvl_n;
-  std::vector<size_t> lvl_smem, lvl_smem_adj;
+  std::vector<int> lvl_off, lvl_n, lvlh_off, lvlh_n;
+  std::vector<size_t> lvl_smem, lvl_smem_adj, lvlh_smem, lvlh_smem_adj;
   std::vector<int64_t> fam_tab;
   std::vector<int32_t> fam_w, fam_col, fam_ncol;
   std::vector<int> nrow;
@@ -991,7 +1032,6 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
   PackOptions2 opt;
   opt.adjoint = (flags & WG_BATCH_GRAD) != 0;
   opt.keep_tables = (flags & (WG_BATCH_GRAD | WG_BATCH_TABLES)) != 0;
-  opt.nt = kNT2;
   Packed2 P = pack_batch2(*m, cs, opt);
   if ((size_t)P.max_smem * sizeof(double) > ctx->smem_optin)
     throw Error(WG_ERANGE, "a task needs more shared memory than one CTA can hold");
@@ -1018,6 +1058,11 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
     b->lvl_smem.push_back((size_t)P.level_smem[L] * sizeof(double));
     b->lvl_smem_adj.push_back((size_t)P.level_smem_adj[L] * sizeof(double));
     lists.insert(lists.end(), P.levels[L].begin(), P.levels[L].end());
+    b->lvlh_off.push_back((int)lists.size());
+    b->lvlh_n.push_back((int)P.levels_h[L].size());
+    b->lvlh_smem.push_back((size_t)P.level_smem_h[L] * sizeof(double));
+    b->lvlh_smem_adj.push_back((size_t)P.level_smem_adj_h[L] * sizeof(double));
+    lists.insert(lists.end(), P.levels_h[L].begin(), P.levels_h[L].end());
   }
   cudaStream_t s = ctx->stream;
   int64_t& by = b->device_bytes;
@@ -1097,25 +1142,52 @@ void enqueue(wg_batch* b, const wg_model* m, bool grad) {
   const bool tables = grad || (b->flags & WG_BATCH_TABLES);
   if (tm) ck(cudaEventRecord(ctx->ev[0], s), "event");
   const int H = (int)b->lvl_n.size();
+  cudaStream_t s2 = ctx->stream2;
+  // one level: heavy tasks (kNT2H threads) on the second stream, light ones
+  // (kNT2L threads) on the main stream, joined before the next level
+  auto level = [&](int L, auto light, auto heavy) {
+    const bool h = b->lvlh_n[L] > 0, l = b->lvl_n[L] > 0;
+    if (h && l) {
+      ck(cudaEventRecord(ctx->fork, s), "event");
+      ck(cudaStreamWaitEvent(s2, ctx->fork, 0), "wait");
+      heavy(s2);
+      light(s);
+      ck(cudaEventRecord(ctx->join, s2), "event");
+      ck(cudaStreamWaitEvent(s, ctx->join, 0), "wait");
+    } else if (h) {
+      heavy(s);
+    } else if (l) {
+      light(s);
+    }
+  };
   for (int L = 0; L < H; ++L) {
-    if (b->lvl_n[L] == 0) continue;
-    const int* list = b->d_lists + b->lvl_off[L];
-    if (tables)
-      k_fwd2<true><<<b->lvl_n[L], kNT2, b->lvl_smem[L], s>>>(A, list);
-    else
-      k_fwd2<false><<<b->lvl_n[L], kNT2, b->lvl_smem[L], s>>>(A, list);
+    const int* ll = b->d_lists + b->lvl_off[L];
+    const int* lh = b->d_lists + b->lvlh_off[L];
+    level(
+        L,
+        [&](cudaStream_t st) {
+          if (tables) k_fwd2<true, kNT2L><<<b->lvl_n[L], kNT2L, b->lvl_smem[L], st>>>(A, ll);
+          else k_fwd2<false, kNT2L><<<b->lvl_n[L], kNT2L, b->lvl_smem[L], st>>>(A, ll);
+        },
+        [&](cudaStream_t st) {
+          if (tables) k_fwd2<true, kNT2H><<<b->lvlh_n[L], kNT2H, b->lvlh_smem[L], st>>>(A, lh);
+          else k_fwd2<false, kNT2H><<<b->lvlh_n[L], kNT2H, b->lvlh_smem[L], st>>>(A, lh);
+        });
   }
   ck(cudaGetLastError(), "forward launch");
   if (tm) ck(cudaEventRecord(ctx->ev[1], s), "event");
   if (grad) {
     ck(cudaMemsetAsync(b->d_gout, 0, sizeof(double) * (size_t)b->gout_doubles, s), "memset");
     for (int L = H - 1; L >= 0; --L) {
-      if (b->lvl_n[L] == 0) continue;
-      k_adj2<<<b->lvl_n[L], kNT2, b->lvl_smem_adj[L], s>>>(A, b->d_lists + b->lvl_off[L]);
+      const int* ll = b->d_lists + b->lvl_off[L];
+      const int* lh = b->d_lists + b->lvlh_off[L];
+      level(
+          L, [&](cudaStream_t st) { k_adj2<kNT2L><<<b->lvl_n[L], kNT2L, b->lvl_smem_adj[L], st>>>(A, ll); },
+          [&](cudaStream_t st) { k_adj2<kNT2H><<<b->lvlh_n[L], kNT2H, b->lvlh_smem_adj[L], st>>>(A, lh); });
     }
     ck(cudaGetLastError(), "adjoint launch");
     if (tm) ck(cudaEventRecord(ctx->ev[2], s), "event");
-    k_reduce2<<<(b->P + 127) / 128, 128, 0, s>>>(b->d_gout, b->d_red_off, b->d_red_idx, b->P, b->d_gred);
+    k_reduce2<<<(b->P * 32 + 255) / 256, 256, 0, s>>>(b->d_gout, b->d_red_off, b->d_red_idx, b->P, b->d_gred);
     ck(cudaGetLastError(), "reduce launch");
     if (tm) ck(cudaEventRecord(ctx->ev[3], s), "event");
   }
@@ -1190,9 +1262,15 @@ int wg_ctx_create(int device, wg_ctx** out) {
     ck(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "attr");
     c->smem_optin = (size_t)v;
     ck(cudaFuncSetAttribute(k_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_fwd2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_fwd2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_adj2, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    ck(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaFuncSetAttribute(k_fwd2<false, kNT2L>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    ck(cudaFuncSetAttribute(k_fwd2<true, kNT2L>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    ck(cudaFuncSetAttribute(k_fwd2<false, kNT2H>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    ck(cudaFuncSetAttribute(k_fwd2<true, kNT2H>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    ck(cudaFuncSetAttribute(k_adj2<kNT2L>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    ck(cudaFuncSetAttribute(k_adj2<kNT2H>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
     *out = c.release();
   });
 }
@@ -1202,6 +1280,9 @@ int wg_ctx_destroy(wg_ctx* ctx) {
   cudaSetDevice(ctx->device);
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
+  if (ctx->fork) cudaEventDestroy(ctx->fork);
+  if (ctx->join) cudaEventDestroy(ctx->join);
+  if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return WG_OK;

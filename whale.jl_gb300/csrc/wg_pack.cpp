@@ -531,7 +531,7 @@ inline double bits_to_double(uint64_t b) {
 // Lane programs with fused finalize.  An item (one clade) is its products
 // followed by its finalize op; items longer than J ops are split into
 // segments ending in FIN_PART, finished by a combine entry after a barrier.
-DProg2 schedule2(std::vector<Item>& items, int ntmax, std::vector<DEntry>& out) {
+DProg2 schedule2(std::vector<Item>& items, int ntmax, int target_j, std::vector<DEntry>& out) {
   DProg2 pr;
   pr.off = (int64_t)out.size();
   int64_t W = 0;
@@ -541,13 +541,9 @@ DProg2 schedule2(std::vector<Item>& items, int ntmax, std::vector<DEntry>& out) 
     maxops = std::max(maxops, (int)it.prods.size() + 1);
   }
   if (W == 0) return pr;
-  int best_w = 1;
-  int64_t best_cost = INT64_MAX;
-  for (int w = 1; w <= ntmax / 32; ++w) {
-    const int64_t J = (W + 32 * w - 1) / (32 * w);
-    const int64_t cost = J * w;
-    if (cost <= best_cost) { best_cost = cost; best_w = w; }  // ties: more warps, shorter rows
-  }
+  // rows are latency-bound: enough warps to bring a row to ~target_j
+  // iterations, no more (idle warps issue nothing, partial ones waste FP64)
+  const int best_w = (int)std::min<int64_t>(ntmax / 32, std::max<int64_t>(1, (W + 32 * target_j - 1) / (32 * target_j)));
   const int NB = 32 * best_w;
   int J = (int)((W + NB - 1) / NB);
   struct Seg { int item, k, begin, len; bool split; };
@@ -671,12 +667,14 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
     H = std::max(H, height[k]);
   }
   P.levels.assign(H + 1, {});
+  P.levels_h.assign(H + 1, {});
   P.level_smem.assign(H + 1, 0);
   P.level_smem_adj.assign(H + 1, 0);
+  P.level_smem_h.assign(H + 1, 0);
+  P.level_smem_adj_h.assign(H + 1, 0);
   // gradient reduction contributions
   std::vector<std::vector<int64_t>> red(3 * (size_t)NR + K + 1);
   auto eps_top_row = [&](int k) { return m.row_off[k] + m.nrow[k] - 1; };
-  const int NT = opt.nt;
 
   for (int k = 0; k < K; ++k) {
     const int kind = m.kind[k];
@@ -695,6 +693,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
     std::stable_sort(fw.begin(), fw.end(), [](auto& x, auto& y) { return x.first > y.first; });
     // next-fit into tasks
     std::vector<std::vector<int>> groups;
+    std::vector<double> group_ops;
     {
       std::vector<int> cur;
       double ops = 0;
@@ -703,6 +702,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
         const int C = info[f].ncompat[k];
         if (!cur.empty() && (ops + w > opt.target_ops || width + C > opt.max_width)) {
           groups.push_back(cur);
+          group_ops.push_back(ops);
           cur.clear();
           ops = 0;
           width = 0;
@@ -711,13 +711,19 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
         ops += w;
         width += C;
       }
-      if (!cur.empty()) groups.push_back(cur);
+      if (!cur.empty()) { groups.push_back(cur); group_ops.push_back(ops); }
     }
-    for (auto& fams : groups) {
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+      const auto& fams = groups[gi];
       const int nf = (int)fams.size();
       DTask T;
       T.node = k;
       T.nfam = nf;
+      const double gops = group_ops[gi];
+      // the root row is a chain of small same-row levels: latency-bound, so
+      // root tasks stay in narrow CTAs that pack densely on the SMs
+      const int NT = (kind != WG_NODE_ROOT && gops > opt.heavy_ops) ? kNT2H : kNT2L;
+      T.nt = NT;
       std::vector<int> col(nf + 1, 0), cola(nf + 1, 0), colb(nf + 1, 0);
       for (int i = 0; i < nf; ++i) {
         col[i + 1] = col[i] + info[fams[i]].ncompat[k];
@@ -789,8 +795,8 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
             items.push_back(std::move(it));
           }
         }
-        if (has_rows) T.dup = schedule2(items, NT, P.entries);
-        if (opt.adjoint) T.tdup = schedule2(titems, NT, P.entries);
+        if (has_rows) T.dup = schedule2(items, NT, opt.target_j, P.entries);
+        if (opt.adjoint) T.tdup = schedule2(titems, NT, opt.target_j, P.entries);
       }
       if (kind == WG_NODE_LEAF) {
         std::vector<int> aux(R, 0);
@@ -820,7 +826,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
             items.push_back(std::move(it));
           }
         }
-        T.init = schedule2(items, NT, P.entries);
+        T.init = schedule2(items, NT, opt.target_j, P.entries);
       } else {
         // speciation + loss (internal) or Πspec + Πloss of the root row
         std::vector<Item> items;
@@ -863,13 +869,13 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
             items.push_back(std::move(it));
           }
         }
-        T.init = schedule2(items, NT, P.entries);
+        T.init = schedule2(items, NT, opt.target_j, P.entries);
         T.loss = put_int2(P.meta, loss);
         if (opt.adjoint) {
           for (int x = 0; x < T.wa; ++x) ta[x].fa = inva[x] < 0 ? 0xFFFF : inva[x];
           for (int x = 0; x < T.wb; ++x) tb[x].fa = invb[x] < 0 ? 0xFFFF : invb[x];
-          T.ta = schedule2(ta, NT, P.entries);
-          T.tb = schedule2(tb, NT, P.entries);
+          T.ta = schedule2(ta, NT, opt.target_j, P.entries);
+          T.tb = schedule2(tb, NT, opt.target_j, P.entries);
           T.inva = put_int(P.meta, inva);
           T.invb = put_int(P.meta, invb);
         }
@@ -907,10 +913,10 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
           for (int x = 0; x < R; ++x) tlw[plevel[x]].push_back(std::move(tby[x]));
         T.nlvl = nl;
         T.lvl = (int64_t)P.progs.size();
-        for (int L = 0; L < nl; ++L) P.progs.push_back(schedule2(lw[L], NT, P.entries));
+        for (int L = 0; L < nl; ++L) P.progs.push_back(schedule2(lw[L], NT, opt.target_j, P.entries));
         if (opt.adjoint) {
           T.tlvl = (int64_t)P.progs.size();
-          for (int L = 0; L < nl; ++L) P.progs.push_back(schedule2(tlw[L], NT, P.entries));
+          for (int L = 0; L < nl; ++L) P.progs.push_back(schedule2(tlw[L], NT, opt.target_j, P.entries));
         }
         std::vector<std::array<int, 2>> fam(nf);
         for (int i = 0; i < nf; ++i) fam[i] = {fams[i], pos(i, ccds[fams[i]]->n_clades - 1)};
@@ -922,8 +928,8 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       // forward: cur, nxt (children staged in nxt); adjoint: bar, barn, two
       // L rows, G; then partial slots and reduction scratch
       const int W2 = std::max(R, T.wa + T.wb);
-      T.smem = 2 * W2 + slots + 16 * (opt.nt / 32) + 32;
-      const int smem_adj = 5 * W2 + slots + 16 * (opt.nt / 32) + 32;
+      T.smem = 2 * W2 + slots + 16 * (NT / 32) + 32;
+      const int smem_adj = 5 * W2 + slots + 16 * (NT / 32) + 32;
       if (opt.adjoint) {
         T.gout = P.gout_doubles;
         const int n = m.nrow[k];
@@ -940,23 +946,29 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
           red[eps_top_row(k)].push_back(T.gout + 2 * n + 4);
         }
       }
-      P.levels[height[k]].push_back((int32_t)P.tasks.size());
-      P.level_smem[height[k]] = std::max(P.level_smem[height[k]], T.smem);
+      const int h = height[k];
+      const bool heavy = NT == kNT2H;
+      (heavy ? P.levels_h : P.levels)[h].push_back((int32_t)P.tasks.size());
+      int& sf = (heavy ? P.level_smem_h : P.level_smem)[h];
+      sf = std::max(sf, T.smem);
       P.max_smem = std::max(P.max_smem, T.smem);
       if (opt.adjoint) {
-        P.level_smem_adj[height[k]] = std::max(P.level_smem_adj[height[k]], smem_adj);
+        int& sa = (heavy ? P.level_smem_adj_h : P.level_smem_adj)[h];
+        sa = std::max(sa, smem_adj);
         P.max_smem = std::max(P.max_smem, smem_adj);
       }
       P.tasks.push_back(T);
     }
   }
-  // heaviest tasks first inside each level
-  for (auto& L : P.levels)
-    std::stable_sort(L.begin(), L.end(), [&](int a, int b) {
-      const DTask& x = P.tasks[a];
-      const DTask& y = P.tasks[b];
-      return (int64_t)x.dup.J * m.nrow[x.node] + x.init.J > (int64_t)y.dup.J * m.nrow[y.node] + y.init.J;
-    });
+  // heaviest tasks first inside each launch
+  auto by_cost = [&](int a, int b) {
+    const DTask& x = P.tasks[a];
+    const DTask& y = P.tasks[b];
+    return (int64_t)(x.dup.J + x.tdup.J) * m.nrow[x.node] + x.init.J >
+           (int64_t)(y.dup.J + y.tdup.J) * m.nrow[y.node] + y.init.J;
+  };
+  for (auto& L : P.levels) std::stable_sort(L.begin(), L.end(), by_cost);
+  for (auto& L : P.levels_h) std::stable_sort(L.begin(), L.end(), by_cost);
   P.red_off.assign(red.size() + 1, 0);
   for (size_t j = 0; j < red.size(); ++j) {
     P.red_off[j + 1] = P.red_off[j] + (int64_t)red[j].size();
