@@ -258,6 +258,7 @@ struct PackOptions2 {
   int target_j = 3;           // iterations per row the lane scheduler aims for
   bool keep_tables = false;
   bool adjoint = false;
+  const std::vector<int>* global_ids = nullptr;  // family index written to log L outputs
 };
 
 Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const PackOptions2& opt);

@@ -369,6 +369,64 @@ __device__ __forceinline__ void run_rows(const DEntry* __restrict__ E, const DPr
   }
 }
 
+// A lane's share of a row program held in registers for all rows of a node:
+// (f0 | f1 << 16, f2 | op << 16, p) per iteration.  Rows then issue no entry
+// loads; operand loads of every iteration are known up front.
+template <int MAXJ>
+struct LaneProg {
+  uint32_t ab[MAXJ];
+  uint32_t om[MAXJ];
+  double p[MAXJ];
+  int J;
+};
+
+template <int MAXJ>
+__device__ __forceinline__ void load_lane_prog(const DEntry* __restrict__ E, const DProg2& pr, int lane,
+                                               LaneProg<MAXJ>& lp) {
+  lp.J = lane < pr.nt ? pr.J : 0;
+  const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + pr.off) + lane;
+#pragma unroll
+  for (int j = 0; j < MAXJ; ++j) {
+    if (j < lp.J) {
+      const ulonglong2 r = __ldg(e + (size_t)j * pr.nt);
+      lp.ab[j] = (uint32_t)(r.x & 0xFFFFFFFFu);
+      lp.om[j] = (uint32_t)((r.x >> 32) & 0xFFFFu) | ((uint32_t)((r.x >> 48) & 0xFFu) << 16);
+      lp.p[j] = __longlong_as_double((long long)r.y);
+    } else {
+      lp.ab[j] = 0;
+      lp.om[j] = (uint32_t)op::NOP << 16;
+      lp.p[j] = 0.0;
+    }
+  }
+}
+
+// One row from a register-resident program.  PROD: acc = fma(p·A[f0], B[f1],
+// acc); the finalize op FIN (entries with f0 = f1 = c): v = fma(ψ, acc,
+// ϕ·A[c]), handed to onfin(c, v, acc); FIN_PART: part[f2] = acc.
+template <int MAXJ, unsigned FIN, class OnFin>
+__device__ __forceinline__ void rows_reg(const LaneProg<MAXJ>& lp, const double* A, const double* B, double* part,
+                                         double ph, double ps, OnFin onfin) {
+  double acc = 0.0;
+#pragma unroll
+  for (int j = 0; j < MAXJ; ++j) {
+    if (j < lp.J) {
+      const unsigned f0 = lp.ab[j] & 0xFFFFu, f1 = lp.ab[j] >> 16, opc = lp.om[j] >> 16;
+      const bool fin = opc == FIN;
+      const double m = (fin ? ph : lp.p[j]) * A[f0];
+      const double v = fma(fin ? ps : m, fin ? acc : B[f1], fin ? m : acc);
+      if (opc == op::PROD) {
+        acc = v;
+      } else if (fin) {
+        onfin(f0, v, acc);
+        acc = 0.0;
+      } else if (opc == op::FIN_PART) {
+        part[lp.om[j] & 0xFFFFu] = acc;
+        acc = 0.0;
+      }
+    }
+  }
+}
+
 __device__ __forceinline__ double eps_top2(const KArgs2& A, int k) {
   return A.params[A.row_off[k] + A.mnode[k].w - 1];
 }
@@ -441,10 +499,22 @@ __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restri
   if (TABLES)
     for (int c = tid; c < R; c += NT) A.tabs[T.tab + c] = cur[c];
   if (mn.x != WG_NODE_ROOT) {
+    constexpr int MAXJ = NT == kNT2L ? 8 : 16;
+    LaneProg<MAXJ> lp;
+    const bool inreg = T.dup.J <= MAXJ;
+    if (inreg) load_lane_prog<MAXJ>(E, T.dup, lane, lp);
     for (int r = 1; r < mn.w; ++r) {
       const double ph = A.params[NR + roff + r], ps = A.params[2 * NR + roff + r];
       double* tr = TABLES ? A.tabs + T.tab + (int64_t)r * R : nullptr;
-      run_rows<TABLES>(E, T.dup, lane, cur, nxt, part, ph, ps, tr);
+      if (inreg) {
+        double* o = nxt;
+        rows_reg<MAXJ, op::FIN_DUP>(lp, cur, cur, part, ph, ps, [&](unsigned c, double v, double) {
+          o[c] = v;
+          if (TABLES) tr[c] = v;
+        });
+      } else {
+        run_rows<TABLES>(E, T.dup, lane, cur, nxt, part, ph, ps, tr);
+      }
       if (T.dup.ncomb) {
         __syncthreads();
         auto cfin = [&](unsigned, unsigned c, unsigned, unsigned, double s) {
@@ -533,7 +603,7 @@ __device__ __forceinline__ void block_sum4(double (&v)[4], double* red) {
 // [2r] ∂/∂ϕ_r, [2r+1] ∂/∂ψ_r (rows r >= 1), [2n] ∂/∂ε_top(child 0),
 // [2n+1] ∂/∂ε_top(child 1), [2n+2] ∂/∂q, [2n+3] ∂/∂η, [2n+4] ∂/∂ε_top(own).
 template <int NT>
-__global__ void __launch_bounds__(NT, NT == 128 ? 8 : 2) k_adj2(const KArgs2 A, const int* __restrict__ list) {
+__global__ void __launch_bounds__(NT, NT == 128 ? 6 : 2) k_adj2(const KArgs2 A, const int* __restrict__ list) {
   extern __shared__ double sm[];
   const DTask& T = A.tasks[list[blockIdx.x]];
   const int k = T.node;
@@ -646,6 +716,10 @@ __global__ void __launch_bounds__(NT, NT == 128 ? 8 : 2) k_adj2(const KArgs2 A, 
 #pragma unroll
   for (int i = 0; i < 8; ++i) rp[i] = rs[i] = 0.0;
   const int wid = tid >> 5, wl = tid & 31;
+  constexpr int MAXJ = NT == kNT2L ? 8 : 16;
+  LaneProg<MAXJ> lp;
+  const bool inreg = T.tdup.J <= MAXJ && n > 1;
+  if (inreg) load_lane_prog<MAXJ>(E, T.tdup, lane, lp);
   for (int r = n - 1; r >= 1; --r) {
     double* Lp = ((n - 1 - r) & 1) ? L1 : L0;
     const double* lr = A.tabs + T.tab + (int64_t)(r - 1) * R;
@@ -653,7 +727,13 @@ __global__ void __launch_bounds__(NT, NT == 128 ? 8 : 2) k_adj2(const KArgs2 A, 
     __syncthreads();
     const double ph = A.params[NR + roff + r], ps = A.params[2 * NR + roff + r];
     // products G[x] = Σ p·bar[γ]·L[sib] and bar_{r-1}[x] = ϕ bar[x] + ψ G[x]
-    if (lane < T.tdup.nt) {
+    if (inreg) {
+      double* bn = barn;
+      rows_reg<MAXJ, op::FIN_ADJ>(lp, bar, Lp, part, ph, ps, [&](unsigned c, double v, double g) {
+        bn[c] = v;
+        Gs[c] = g;
+      });
+    } else if (lane < T.tdup.nt) {
       const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + T.tdup.off) + lane;
       double acc = 0.0;
       for (int j = 0; j < T.tdup.J; ++j, e += T.tdup.nt) {
@@ -898,18 +978,18 @@ struct PlainBatch {
   }
 };
 
-// Batched path: level-synchronous (node, family group) tasks.
-struct wg_batch {
-  wg_ctx* ctx = nullptr;
-  int K = 0, NR = 0, NF = 0, P = 0, n_tasks = 0;
-  uint32_t flags = 0;
-  int64_t device_bytes = 0;
-  double flops_fwd = 0, bytes_fwd = 0, flops_adj = 0;
+// Batched path: families split into size classes; each class is a layout of
+// level-synchronous (node, family group) tasks on its own pair of streams, so
+// the classes overlap on the device and every launch sizes its shared memory
+// for tasks of one size class.
+struct SubBatch {
+  int device = 0;
+  int n_tasks = 0;
+  std::vector<int> fam;  // global family index of each local family
   std::vector<int> lvl_off, lvl_n, lvlh_off, lvlh_n;
   std::vector<size_t> lvl_smem, lvl_smem_adj, lvlh_smem, lvlh_smem_adj;
   std::vector<int64_t> fam_tab;
   std::vector<int32_t> fam_w, fam_col, fam_ncol;
-  std::vector<int> nrow;
   DTask* d_tasks = nullptr;
   DEntry* d_entries = nullptr;
   int* d_meta = nullptr;
@@ -918,29 +998,55 @@ struct wg_batch {
   int* d_lists = nullptr;
   int64_t* d_red_off = nullptr;
   int64_t* d_red_idx = nullptr;
-  int4* d_mnode = nullptr;
-  int* d_rowoff = nullptr;
-  double* d_leafp = nullptr;
-  double* d_params = nullptr;
   double* d_tops = nullptr;
   double* d_tabs = nullptr;
   double* d_bartops = nullptr;
   double* d_gout = nullptr;
   double* d_gred = nullptr;
-  double* d_logl = nullptr;
   int64_t gout_doubles = 0;
+  cudaStream_t s = nullptr, s2 = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr, done = nullptr;
+  ~SubBatch() {
+    free_all(device, {d_tasks, d_entries, d_meta, d_gmap, d_progs, d_lists, d_red_off, d_red_idx, d_tops, d_tabs,
+                      d_bartops, d_gout, d_gred},
+             {});
+    for (cudaEvent_t e : {fork, join, done})
+      if (e) cudaEventDestroy(e);
+    if (s2) cudaStreamDestroy(s2);
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
+struct wg_batch {
+  wg_ctx* ctx = nullptr;
+  int K = 0, NR = 0, NF = 0, P = 0, n_tasks = 0;
+  uint32_t flags = 0;
+  int64_t device_bytes = 0;
+  double flops_fwd = 0, bytes_fwd = 0, flops_adj = 0;
+  std::vector<std::unique_ptr<SubBatch>> subs;
+  std::vector<int> fam_sub, fam_local;
+  std::vector<int> nrow;
+  int4* d_mnode = nullptr;
+  int* d_rowoff = nullptr;
+  double* d_leafp = nullptr;
+  double* d_params = nullptr;
+  double* d_logl = nullptr;
   double* h_params = nullptr;
   double* h_logl = nullptr;
-  double* h_gred = nullptr;
+  double* h_gred = nullptr;  // P per sub-batch
   bool grad_pending = false;
+  bool pending = false;  // an enqueued evaluation has not been fetched yet
   std::vector<wg_ccd*> ccds;  // not owned; for the lazily built plain layout
   std::unique_ptr<PlainBatch> plain;
+  // captured launch sequences: [with gradient][with tables]
+  cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   ~wg_batch() {
+    for (auto& g2 : graph)
+      for (auto& g : g2)
+        if (g) cudaGraphExecDestroy(g);
     plain.reset();
-    if (ctx)
-      free_all(ctx->device, {d_tasks, d_entries, d_meta, d_gmap, d_progs, d_lists, d_red_off, d_red_idx, d_mnode,
-                             d_rowoff, d_leafp, d_params, d_tops, d_tabs, d_bartops, d_gout, d_gred, d_logl},
-               {h_params, h_logl, h_gred});
+    subs.clear();
+    if (ctx) free_all(ctx->device, {d_mnode, d_rowoff, d_leafp, d_params, d_logl}, {h_params, h_logl, h_gred});
   }
 };
 
@@ -1022,19 +1128,13 @@ KArgs plain_args(const PlainBatch* b) {
   return A;
 }
 
+// Size classes by clade count (upper bounds); one layout per non-empty class.
+constexpr int kClassBounds[] = {256, 1024, 1 << 30};
+
 std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* const* ccds, int n, uint32_t flags) {
   ck(cudaSetDevice(ctx->device), "cudaSetDevice");
-  std::vector<const CCD*> cs;
-  for (int i = 0; i < n; ++i) {
+  for (int i = 0; i < n; ++i)
     if (!ccds[i]) throw Error(WG_EINVAL, "null CCD in batch");
-    cs.push_back(ccds[i]);
-  }
-  PackOptions2 opt;
-  opt.adjoint = (flags & WG_BATCH_GRAD) != 0;
-  opt.keep_tables = (flags & (WG_BATCH_GRAD | WG_BATCH_TABLES)) != 0;
-  Packed2 P = pack_batch2(*m, cs, opt);
-  if ((size_t)P.max_smem * sizeof(double) > ctx->smem_optin)
-    throw Error(WG_ERANGE, "a task needs more shared memory than one CTA can hold");
   auto b = std::make_unique<wg_batch>();
   b->ctx = ctx;
   b->K = m->K;
@@ -1042,80 +1142,114 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
   b->NF = n;
   b->flags = flags;
   b->P = 3 * b->NR + b->K + 1;
-  b->n_tasks = (int)P.tasks.size();
-  b->flops_fwd = P.flops_fwd;
-  b->bytes_fwd = P.bytes_fwd;
-  b->flops_adj = P.flops_adj;
-  b->fam_tab = P.fam_tab;
-  b->fam_w = P.fam_w;
-  b->fam_col = P.fam_col;
-  b->fam_ncol = P.fam_ncol;
   b->nrow = m->nrow;
-  std::vector<int> lists;
-  for (size_t L = 0; L < P.levels.size(); ++L) {
-    b->lvl_off.push_back((int)lists.size());
-    b->lvl_n.push_back((int)P.levels[L].size());
-    b->lvl_smem.push_back((size_t)P.level_smem[L] * sizeof(double));
-    b->lvl_smem_adj.push_back((size_t)P.level_smem_adj[L] * sizeof(double));
-    lists.insert(lists.end(), P.levels[L].begin(), P.levels[L].end());
-    b->lvlh_off.push_back((int)lists.size());
-    b->lvlh_n.push_back((int)P.levels_h[L].size());
-    b->lvlh_smem.push_back((size_t)P.level_smem_h[L] * sizeof(double));
-    b->lvlh_smem_adj.push_back((size_t)P.level_smem_adj_h[L] * sizeof(double));
-    lists.insert(lists.end(), P.levels_h[L].begin(), P.levels_h[L].end());
-  }
+  b->fam_sub.assign(n, -1);
+  b->fam_local.assign(n, -1);
   cudaStream_t s = ctx->stream;
   int64_t& by = b->device_bytes;
-  b->d_tasks = dalloc<DTask>(P.tasks.size(), by);
-  b->d_entries = dalloc<DEntry>(P.entries.size(), by);
-  b->d_meta = dalloc<int>(P.meta.size(), by);
-  b->d_gmap = dalloc<int64_t>(P.gmap.size(), by);
-  b->d_progs = dalloc<DProg2>(P.progs.size(), by);
-  b->d_lists = dalloc<int>(lists.size(), by);
-  b->d_params = dalloc<double>(b->P, by);
-  b->d_tops = dalloc<double>(P.tops_doubles, by);
-  if (opt.keep_tables) b->d_tabs = dalloc<double>(P.tab_doubles, by);
-  if (opt.adjoint) {
-    b->d_bartops = dalloc<double>(P.tops_doubles, by);
-    b->gout_doubles = P.gout_doubles;
-    b->d_gout = dalloc<double>(P.gout_doubles, by);
-    b->d_gred = dalloc<double>(b->P, by);
-    b->d_red_off = dalloc<int64_t>(P.red_off.size(), by);
-    b->d_red_idx = dalloc<int64_t>(P.red_idx.size(), by);
-    h2d(b->d_red_off, P.red_off, s);
-    h2d(b->d_red_idx, P.red_idx, s);
+  const bool adjoint = (flags & WG_BATCH_GRAD) != 0;
+  const bool keep = (flags & (WG_BATCH_GRAD | WG_BATCH_TABLES)) != 0;
+  int lo = 0;
+  for (int bound : kClassBounds) {
+    std::vector<int> ids;
+    for (int i = 0; i < n; ++i)
+      if (ccds[i]->n_clades > lo && ccds[i]->n_clades <= bound) ids.push_back(i);
+    lo = bound;
+    if (ids.empty()) continue;
+    std::vector<const CCD*> cs;
+    for (int i : ids) cs.push_back(ccds[i]);
+    PackOptions2 opt;
+    opt.adjoint = adjoint;
+    opt.keep_tables = keep;
+    opt.global_ids = &ids;
+    Packed2 P = pack_batch2(*m, cs, opt);
+    if ((size_t)P.max_smem * sizeof(double) > ctx->smem_optin)
+      throw Error(WG_ERANGE, "a task needs more shared memory than one CTA can hold");
+    auto sb = std::make_unique<SubBatch>();
+    sb->device = ctx->device;
+    sb->fam = ids;
+    sb->n_tasks = (int)P.tasks.size();
+    sb->fam_tab = P.fam_tab;
+    sb->fam_w = P.fam_w;
+    sb->fam_col = P.fam_col;
+    sb->fam_ncol = P.fam_ncol;
+    b->n_tasks += sb->n_tasks;
+    b->flops_fwd += P.flops_fwd;
+    b->bytes_fwd += P.bytes_fwd;
+    b->flops_adj += P.flops_adj;
+    for (size_t i = 0; i < ids.size(); ++i) {
+      b->fam_sub[ids[i]] = (int)b->subs.size();
+      b->fam_local[ids[i]] = (int)i;
+    }
+    std::vector<int> lists;
+    for (size_t L = 0; L < P.levels.size(); ++L) {
+      sb->lvl_off.push_back((int)lists.size());
+      sb->lvl_n.push_back((int)P.levels[L].size());
+      sb->lvl_smem.push_back((size_t)P.level_smem[L] * sizeof(double));
+      sb->lvl_smem_adj.push_back((size_t)P.level_smem_adj[L] * sizeof(double));
+      lists.insert(lists.end(), P.levels[L].begin(), P.levels[L].end());
+      sb->lvlh_off.push_back((int)lists.size());
+      sb->lvlh_n.push_back((int)P.levels_h[L].size());
+      sb->lvlh_smem.push_back((size_t)P.level_smem_h[L] * sizeof(double));
+      sb->lvlh_smem_adj.push_back((size_t)P.level_smem_adj_h[L] * sizeof(double));
+      lists.insert(lists.end(), P.levels_h[L].begin(), P.levels_h[L].end());
+    }
+    sb->d_tasks = dalloc<DTask>(P.tasks.size(), by);
+    sb->d_entries = dalloc<DEntry>(P.entries.size(), by);
+    sb->d_meta = dalloc<int>(P.meta.size(), by);
+    sb->d_gmap = dalloc<int64_t>(P.gmap.size(), by);
+    sb->d_progs = dalloc<DProg2>(P.progs.size(), by);
+    sb->d_lists = dalloc<int>(lists.size(), by);
+    sb->d_tops = dalloc<double>(P.tops_doubles, by);
+    if (keep) sb->d_tabs = dalloc<double>(P.tab_doubles, by);
+    if (adjoint) {
+      sb->d_bartops = dalloc<double>(P.tops_doubles, by);
+      sb->gout_doubles = P.gout_doubles;
+      sb->d_gout = dalloc<double>(P.gout_doubles, by);
+      sb->d_gred = dalloc<double>(b->P, by);
+      sb->d_red_off = dalloc<int64_t>(P.red_off.size(), by);
+      sb->d_red_idx = dalloc<int64_t>(P.red_idx.size(), by);
+      h2d(sb->d_red_off, P.red_off, s);
+      h2d(sb->d_red_idx, P.red_idx, s);
+    }
+    h2d(sb->d_tasks, P.tasks, s);
+    h2d(sb->d_entries, P.entries, s);
+    h2d(sb->d_meta, P.meta, s);
+    h2d(sb->d_gmap, P.gmap, s);
+    h2d(sb->d_progs, P.progs, s);
+    h2d(sb->d_lists, lists, s);
+    ck(cudaStreamCreateWithFlags(&sb->s, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaStreamCreateWithFlags(&sb->s2, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (cudaEvent_t* e : {&sb->fork, &sb->join, &sb->done})
+      ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
+    b->subs.push_back(std::move(sb));
   }
+  b->d_params = dalloc<double>(b->P, by);
   b->d_logl = dalloc<double>(n, by);
-  h2d(b->d_tasks, P.tasks, s);
-  h2d(b->d_entries, P.entries, s);
-  h2d(b->d_meta, P.meta, s);
-  h2d(b->d_gmap, P.gmap, s);
-  h2d(b->d_progs, P.progs, s);
-  h2d(b->d_lists, lists, s);
   upload_model_static(b.get(), m, s);
   ck(cudaMallocHost(&b->h_params, sizeof(double) * b->P), "cudaMallocHost");
   ck(cudaMallocHost(&b->h_logl, sizeof(double) * n), "cudaMallocHost");
-  if (opt.adjoint) ck(cudaMallocHost(&b->h_gred, sizeof(double) * b->P), "cudaMallocHost");
+  if (adjoint) ck(cudaMallocHost(&b->h_gred, sizeof(double) * b->P * b->subs.size()), "cudaMallocHost");
   ck(cudaStreamSynchronize(s), "batch upload");
   b->ccds.assign(ccds, ccds + n);
   return b;
 }
 
-KArgs2 batch_args(const wg_batch* b) {
+KArgs2 sub_args(const wg_batch* b, const SubBatch* sb) {
   KArgs2 A;
-  A.tasks = b->d_tasks;
-  A.entries = b->d_entries;
-  A.meta = b->d_meta;
-  A.gmap = b->d_gmap;
-  A.progs = b->d_progs;
+  A.tasks = sb->d_tasks;
+  A.entries = sb->d_entries;
+  A.meta = sb->d_meta;
+  A.gmap = sb->d_gmap;
+  A.progs = sb->d_progs;
   A.mnode = b->d_mnode;
   A.row_off = b->d_rowoff;
   A.leafp = b->d_leafp;
   A.params = b->d_params;
-  A.tops = b->d_tops;
-  A.tabs = b->d_tabs;
-  A.bartops = b->d_bartops;
-  A.gout = b->d_gout;
+  A.tops = sb->d_tops;
+  A.tabs = sb->d_tabs;
+  A.bartops = sb->d_bartops;
+  A.gout = sb->d_gout;
   A.logl = b->d_logl;
   A.NR = b->NR;
   A.K = b->K;
@@ -1128,107 +1262,166 @@ void check_model(const B* b, const wg_model* m) {
   if (m->K != b->K || m->total_rows() != b->NR) throw Error(WG_EINVAL, "batch was built for a different model");
 }
 
-// Stage the parameters and launch the forward levels (and the reverse levels
-// of the adjoint plus the gradient reduction) on the context stream.
+// One level of one size class: heavy tasks on the class's second stream,
+// light ones on its first, joined before the next level.
+template <class Light, class Heavy>
+void run_level(SubBatch* sb, int L, Light light, Heavy heavy) {
+  const bool h = sb->lvlh_n[L] > 0, l = sb->lvl_n[L] > 0;
+  if (h && l) {
+    ck(cudaEventRecord(sb->fork, sb->s), "event");
+    ck(cudaStreamWaitEvent(sb->s2, sb->fork, 0), "wait");
+    heavy(sb->s2);
+    light(sb->s);
+    ck(cudaEventRecord(sb->join, sb->s2), "event");
+    ck(cudaStreamWaitEvent(sb->s, sb->join, 0), "wait");
+  } else if (h) {
+    heavy(sb->s);
+  } else if (l) {
+    light(sb->s);
+  }
+}
+
+// The context stream forks to every size class and joins them again.
+void fork_subs(wg_batch* b) {
+  wg_ctx* ctx = b->ctx;
+  ck(cudaEventRecord(ctx->fork, ctx->stream), "event");
+  for (auto& sb : b->subs) ck(cudaStreamWaitEvent(sb->s, ctx->fork, 0), "wait");
+}
+void join_subs(wg_batch* b) {
+  wg_ctx* ctx = b->ctx;
+  for (auto& sb : b->subs) {
+    ck(cudaEventRecord(sb->done, sb->s), "event");
+    ck(cudaStreamWaitEvent(ctx->stream, sb->done, 0), "wait");
+  }
+}
+
+// Every class's forward levels (and the reverse levels of the adjoint plus
+// its gradient reduction), forked from and joined back to the context stream.
+void record_sequence(wg_batch* b, bool grad, bool tables) {
+  wg_ctx* ctx = b->ctx;
+  cudaStream_t s = ctx->stream;
+  ck(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(double) * b->P, cudaMemcpyHostToDevice, s), "params upload");
+  if (grad)
+    for (auto& sb : b->subs)
+      ck(cudaMemsetAsync(sb->d_gout, 0, sizeof(double) * (size_t)sb->gout_doubles, s), "memset");
+  ck(cudaEventRecordWithFlags(ctx->ev[0], s, cudaEventRecordExternal), "event");
+  fork_subs(b);
+  for (auto& sbp : b->subs) {
+    SubBatch* sb = sbp.get();
+    const KArgs2 A = sub_args(b, sb);
+    for (int L = 0; L < (int)sb->lvl_n.size(); ++L) {
+      const int* ll = sb->d_lists + sb->lvl_off[L];
+      const int* lh = sb->d_lists + sb->lvlh_off[L];
+      run_level(
+          sb, L,
+          [&](cudaStream_t st) {
+            if (tables) k_fwd2<true, kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem[L], st>>>(A, ll);
+            else k_fwd2<false, kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem[L], st>>>(A, ll);
+          },
+          [&](cudaStream_t st) {
+            if (tables) k_fwd2<true, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], st>>>(A, lh);
+            else k_fwd2<false, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], st>>>(A, lh);
+          });
+    }
+  }
+  ck(cudaGetLastError(), "forward launch");
+  join_subs(b);
+  ck(cudaEventRecordWithFlags(ctx->ev[1], s, cudaEventRecordExternal), "event");
+  if (grad) {
+    fork_subs(b);
+    for (auto& sbp : b->subs) {
+      SubBatch* sb = sbp.get();
+      const KArgs2 A = sub_args(b, sb);
+      for (int L = (int)sb->lvl_n.size() - 1; L >= 0; --L) {
+        const int* ll = sb->d_lists + sb->lvl_off[L];
+        const int* lh = sb->d_lists + sb->lvlh_off[L];
+        run_level(
+            sb, L, [&](cudaStream_t st) { k_adj2<kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem_adj[L], st>>>(A, ll); },
+            [&](cudaStream_t st) { k_adj2<kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem_adj[L], st>>>(A, lh); });
+      }
+      k_reduce2<<<(b->P * 32 + 255) / 256, 256, 0, sb->s>>>(sb->d_gout, sb->d_red_off, sb->d_red_idx, b->P,
+                                                            sb->d_gred);
+    }
+    ck(cudaGetLastError(), "adjoint launch");
+    join_subs(b);
+    ck(cudaEventRecordWithFlags(ctx->ev[2], s, cudaEventRecordExternal), "event");
+    ck(cudaEventRecordWithFlags(ctx->ev[3], s, cudaEventRecordExternal), "event");
+  }
+}
+
+// Stage the parameters on the host and replay the captured launch sequence
+// (captured into a CUDA graph on first use).
 void enqueue(wg_batch* b, const wg_model* m, bool grad) {
   check_model(b, m);
   wg_ctx* ctx = b->ctx;
   ck(cudaSetDevice(ctx->device), "cudaSetDevice");
   if (grad && !(b->flags & WG_BATCH_GRAD)) throw Error(WG_ESTATE, "batch was created without WG_BATCH_GRAD");
-  cudaStream_t s = ctx->stream;
-  const bool tm = ctx->timing;
-  upload_params(m, b->NR, b->K, b->h_params, b->d_params, s);
-  const KArgs2 A = batch_args(b);
+  for (auto& e : ctx->ev)
+    if (!e) ck(cudaEventCreate(&e), "cudaEventCreate");
+  // the pinned parameter buffer is read by the previous launch's copy
+  if (b->pending) ck(cudaStreamSynchronize(ctx->stream), "pending evaluation");
+  const int NR = b->NR, K = b->K;
+  std::memcpy(b->h_params, m->eps.data(), NR * sizeof(double));
+  std::memcpy(b->h_params + NR, m->phi.data(), NR * sizeof(double));
+  std::memcpy(b->h_params + 2 * NR, m->psi.data(), NR * sizeof(double));
+  for (int k = 0; k < K; ++k) b->h_params[3 * NR + k] = std::isnan(m->q[k]) ? 0.0 : m->q[k];
+  b->h_params[3 * NR + K] = m->eta;
   const bool tables = grad || (b->flags & WG_BATCH_TABLES);
-  if (tm) ck(cudaEventRecord(ctx->ev[0], s), "event");
-  const int H = (int)b->lvl_n.size();
-  cudaStream_t s2 = ctx->stream2;
-  // one level: heavy tasks (kNT2H threads) on the second stream, light ones
-  // (kNT2L threads) on the main stream, joined before the next level
-  auto level = [&](int L, auto light, auto heavy) {
-    const bool h = b->lvlh_n[L] > 0, l = b->lvl_n[L] > 0;
-    if (h && l) {
-      ck(cudaEventRecord(ctx->fork, s), "event");
-      ck(cudaStreamWaitEvent(s2, ctx->fork, 0), "wait");
-      heavy(s2);
-      light(s);
-      ck(cudaEventRecord(ctx->join, s2), "event");
-      ck(cudaStreamWaitEvent(s, ctx->join, 0), "wait");
-    } else if (h) {
-      heavy(s);
-    } else if (l) {
-      light(s);
+  cudaGraphExec_t& ge = b->graph[grad][tables];
+  cudaStream_t s = ctx->stream;
+  if (!ge) {
+    ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    try {
+      record_sequence(b, grad, tables);
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
     }
-  };
-  for (int L = 0; L < H; ++L) {
-    const int* ll = b->d_lists + b->lvl_off[L];
-    const int* lh = b->d_lists + b->lvlh_off[L];
-    level(
-        L,
-        [&](cudaStream_t st) {
-          if (tables) k_fwd2<true, kNT2L><<<b->lvl_n[L], kNT2L, b->lvl_smem[L], st>>>(A, ll);
-          else k_fwd2<false, kNT2L><<<b->lvl_n[L], kNT2L, b->lvl_smem[L], st>>>(A, ll);
-        },
-        [&](cudaStream_t st) {
-          if (tables) k_fwd2<true, kNT2H><<<b->lvlh_n[L], kNT2H, b->lvlh_smem[L], st>>>(A, lh);
-          else k_fwd2<false, kNT2H><<<b->lvlh_n[L], kNT2H, b->lvlh_smem[L], st>>>(A, lh);
-        });
+    cudaGraph_t g = nullptr;
+    ck(cudaStreamEndCapture(s, &g), "end capture");
+    const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    ck(e, "graph instantiate");
   }
-  ck(cudaGetLastError(), "forward launch");
-  if (tm) ck(cudaEventRecord(ctx->ev[1], s), "event");
-  if (grad) {
-    ck(cudaMemsetAsync(b->d_gout, 0, sizeof(double) * (size_t)b->gout_doubles, s), "memset");
-    for (int L = H - 1; L >= 0; --L) {
-      const int* ll = b->d_lists + b->lvl_off[L];
-      const int* lh = b->d_lists + b->lvlh_off[L];
-      level(
-          L, [&](cudaStream_t st) { k_adj2<kNT2L><<<b->lvl_n[L], kNT2L, b->lvl_smem_adj[L], st>>>(A, ll); },
-          [&](cudaStream_t st) { k_adj2<kNT2H><<<b->lvlh_n[L], kNT2H, b->lvlh_smem_adj[L], st>>>(A, lh); });
-    }
-    ck(cudaGetLastError(), "adjoint launch");
-    if (tm) ck(cudaEventRecord(ctx->ev[2], s), "event");
-    k_reduce2<<<(b->P * 32 + 255) / 256, 256, 0, s>>>(b->d_gout, b->d_red_off, b->d_red_idx, b->P, b->d_gred);
-    ck(cudaGetLastError(), "reduce launch");
-    if (tm) ck(cudaEventRecord(ctx->ev[3], s), "event");
-  }
-  ctx->timed = tm;
+  ck(cudaGraphLaunch(ge, s), "graph launch");
+  b->pending = true;
+  ctx->timed = ctx->timing;
   ctx->timed_grad = grad;
   b->grad_pending = grad;
 }
 
-template <class B>
-void fetch(B* b, const wg_model* m, double* per_family, double* total, double* d_lam, double* d_mu, double* d_q,
-           double* d_eta, double* d_eps, double* d_phi, double* d_psi) {
-  cudaStream_t s = b->ctx->stream;
-  ck(cudaMemcpyAsync(b->h_logl, b->d_logl, sizeof(double) * b->NF, cudaMemcpyDeviceToHost, s), "logl download");
-  const bool grad = b->grad_pending;
-  if (grad)
-    ck(cudaMemcpyAsync(b->h_gred, b->d_gred, sizeof(double) * b->P, cudaMemcpyDeviceToHost, s), "grad download");
-  ck(cudaStreamSynchronize(s), "evaluation");
-  wg_ctx* ctx = b->ctx;
-  if (ctx->timed) {
-    ck(cudaEventElapsedTime(&ctx->last_ms[0], ctx->ev[0], ctx->ev[1]), "event time");
-    ctx->last_ms[1] = ctx->last_ms[2] = 0.0f;
-    if (ctx->timed_grad) {
-      ck(cudaEventElapsedTime(&ctx->last_ms[1], ctx->ev[1], ctx->ev[2]), "event time");
-      ck(cudaEventElapsedTime(&ctx->last_ms[2], ctx->ev[2], ctx->ev[3]), "event time");
-    }
-    ctx->timed = false;
+void finish_timing(wg_ctx* ctx) {
+  if (!ctx->timed) return;
+  ck(cudaEventElapsedTime(&ctx->last_ms[0], ctx->ev[0], ctx->ev[1]), "event time");
+  ctx->last_ms[1] = ctx->last_ms[2] = 0.0f;
+  if (ctx->timed_grad) {
+    ck(cudaEventElapsedTime(&ctx->last_ms[1], ctx->ev[1], ctx->ev[2]), "event time");
+    ck(cudaEventElapsedTime(&ctx->last_ms[2], ctx->ev[2], ctx->ev[3]), "event time");
   }
+  ctx->timed = false;
+}
+
+// Per-family log L, the conditioned total and (for a gradient evaluation) the
+// chain from the table adjoints to the rates, on the host.
+void finish(const wg_model* m, int NF, const double* logl, const double* gred, bool grad, double* per_family,
+            double* total, double* d_lam, double* d_mu, double* d_q, double* d_eta, double* d_eps, double* d_phi,
+            double* d_psi) {
   // sum over families minus N * condition, ℓhood (src/core.jl:15, :58-64)
   double sum = 0.0;
-  for (int i = 0; i < b->NF; ++i) sum += b->h_logl[i];
+  for (int i = 0; i < NF; ++i) sum += logl[i];
   const double cond = model_condition(*m);
-  double tot = sum - b->NF * cond;
+  double tot = sum - NF * cond;
   if (!std::isfinite(tot)) tot = -INFINITY;
-  if (per_family) std::memcpy(per_family, b->h_logl, sizeof(double) * b->NF);
+  if (per_family) std::memcpy(per_family, logl, sizeof(double) * NF);
   if (total) *total = tot;
   if (!grad) return;
-  const int NR = b->NR, K = b->K;
-  std::vector<double> de(b->h_gred, b->h_gred + NR), dp(b->h_gred + NR, b->h_gred + 2 * NR),
-      ds(b->h_gred + 2 * NR, b->h_gred + 3 * NR), dq(b->h_gred + 3 * NR, b->h_gred + 3 * NR + K);
-  double deta = b->h_gred[3 * NR + K];
-  model_condition_vjp(*m, -(double)b->NF, de, deta);
+  const int NR = m->total_rows(), K = m->K;
+  std::vector<double> de(gred, gred + NR), dp(gred + NR, gred + 2 * NR), ds(gred + 2 * NR, gred + 3 * NR),
+      dq(gred + 3 * NR, gred + 3 * NR + K);
+  double deta = gred[3 * NR + K];
+  model_condition_vjp(*m, -(double)NF, de, deta);
   if (d_eps) std::memcpy(d_eps, de.data(), NR * sizeof(double));
   if (d_phi) std::memcpy(d_phi, dp.data(), NR * sizeof(double));
   if (d_psi) std::memcpy(d_psi, ds.data(), NR * sizeof(double));
@@ -1240,6 +1433,36 @@ void fetch(B* b, const wg_model* m, double* per_family, double* total, double* d
     if (d_mu) std::memcpy(d_mu, dm.data(), K * sizeof(double));
   }
   if (d_q) std::memcpy(d_q, dq.data(), K * sizeof(double));
+}
+
+void fetch(wg_batch* b, const wg_model* m, double* per_family, double* total, double* d_lam, double* d_mu,
+           double* d_q, double* d_eta, double* d_eps, double* d_phi, double* d_psi) {
+  cudaStream_t s = b->ctx->stream;
+  ck(cudaMemcpyAsync(b->h_logl, b->d_logl, sizeof(double) * b->NF, cudaMemcpyDeviceToHost, s), "logl download");
+  const bool grad = b->grad_pending;
+  if (grad)
+    for (size_t i = 0; i < b->subs.size(); ++i)
+      ck(cudaMemcpyAsync(b->h_gred + i * b->P, b->subs[i]->d_gred, sizeof(double) * b->P, cudaMemcpyDeviceToHost, s),
+         "grad download");
+  ck(cudaStreamSynchronize(s), "evaluation");
+  b->pending = false;
+  finish_timing(b->ctx);
+  std::vector<double> gred;
+  if (grad) {  // size classes summed in class order
+    gred.assign(b->h_gred, b->h_gred + b->P);
+    for (size_t i = 1; i < b->subs.size(); ++i)
+      for (int j = 0; j < b->P; ++j) gred[j] += b->h_gred[i * b->P + j];
+  }
+  finish(m, b->NF, b->h_logl, gred.data(), grad, per_family, total, d_lam, d_mu, d_q, d_eta, d_eps, d_phi, d_psi);
+}
+
+void fetch_plain(PlainBatch* b, const wg_model* m, double* per_family, double* total) {
+  cudaStream_t s = b->ctx->stream;
+  ck(cudaMemcpyAsync(b->h_logl, b->d_logl, sizeof(double) * b->NF, cudaMemcpyDeviceToHost, s), "logl download");
+  ck(cudaStreamSynchronize(s), "evaluation");
+  finish_timing(b->ctx);
+  finish(m, b->NF, b->h_logl, nullptr, false, per_family, total, nullptr, nullptr, nullptr, nullptr, nullptr,
+         nullptr, nullptr);
 }
 
 }  // namespace
@@ -1396,8 +1619,7 @@ int wg_logpdf_plain(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, d
       k_forward<false><<<1, kNT, pb->smem_fwd, s>>>(A);
     }
     ck(cudaGetLastError(), "plain launch");
-    pb->grad_pending = false;
-    fetch(pb, m, per_family, total, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    fetch_plain(pb, m, per_family, total);
   });
 }
 
@@ -1408,8 +1630,10 @@ int wg_logpdf_tables(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t family, doub
     if (family < 0 || family >= b->NF) throw Error(WG_EINVAL, "family index out of range");
     if (!(b->flags & WG_BATCH_TABLES)) throw Error(WG_ESTATE, "batch was created without WG_BATCH_TABLES");
     const int K = b->K;
+    const SubBatch* sb = b->subs[b->fam_sub[family]].get();
+    const size_t lf = (size_t)b->fam_local[family];
     int64_t need = 0;
-    for (int k = 0; k < K; ++k) need += (int64_t)b->nrow[k] * b->fam_ncol[(size_t)family * K + k];
+    for (int k = 0; k < K; ++k) need += (int64_t)b->nrow[k] * sb->fam_ncol[lf * K + k];
     if (needed) *needed = need;
     if (!out) return WG_OK;
     if (cap < need) throw Error(WG_ERANGE, "output buffer too small");
@@ -1419,11 +1643,11 @@ int wg_logpdf_tables(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t family, doub
     cudaStream_t s = ctx->stream;
     int64_t o = 0;
     for (int k = 0; k < K; ++k) {
-      const size_t fk = (size_t)family * K + k;
-      const int nc = b->fam_ncol[fk];
+      const size_t fk = lf * K + k;
+      const int nc = sb->fam_ncol[fk];
       if (nc > 0)
-        ck(cudaMemcpy2DAsync(out + o, nc * sizeof(double), b->d_tabs + b->fam_tab[fk] + b->fam_col[fk],
-                             (size_t)b->fam_w[fk] * sizeof(double), nc * sizeof(double), b->nrow[k],
+        ck(cudaMemcpy2DAsync(out + o, nc * sizeof(double), sb->d_tabs + sb->fam_tab[fk] + sb->fam_col[fk],
+                             (size_t)sb->fam_w[fk] * sizeof(double), nc * sizeof(double), b->nrow[k],
                              cudaMemcpyDeviceToHost, s),
            "table download");
       o += (int64_t)b->nrow[k] * nc;

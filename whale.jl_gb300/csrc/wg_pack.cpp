@@ -919,7 +919,8 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
           for (int L = 0; L < nl; ++L) P.progs.push_back(schedule2(tlw[L], NT, opt.target_j, P.entries));
         }
         std::vector<std::array<int, 2>> fam(nf);
-        for (int i = 0; i < nf; ++i) fam[i] = {fams[i], pos(i, ccds[fams[i]]->n_clades - 1)};
+        for (int i = 0; i < nf; ++i)
+          fam[i] = {opt.global_ids ? (*opt.global_ids)[fams[i]] : fams[i], pos(i, ccds[fams[i]]->n_clades - 1)};
         T.fam = put_int2(P.meta, fam);
       }
       // shared memory: cur + nxt rows (children staged in nxt) + slots + spare
