@@ -168,6 +168,21 @@ int wg_logpdf_plain(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, d
 int wg_logpdf_tables(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t family, double* out, int64_t cap,
                      int64_t* needed, double* logl);
 
+/* Forward evaluation that allocates nothing (no counterpart in the reference).
+ * For callers that cannot allocate device memory when they evaluate: hosts
+ * whose device memory is owned by another allocator or pool, and sampler
+ * loops that must not enter the allocator between steps (cudaMalloc can
+ * synchronise the device and fail under memory pressure).  Same results
+ * as wg_logpdf on a batch created beforehand (any flags).  The scratch it
+ * needs -- the top row of every (node, family group) task -- lives in one
+ * fixed device array of 1 << 20 doubles (8 MiB) that every GPU loading the
+ * library holds until exit; batches needing more are rejected with WG_ERANGE.
+ * The first call on a device looks up that array's address (no allocation),
+ * so make it before any stream capture.  All calls share the array and it
+ * keeps the last call's contents: calls whose work overlaps on the GPU (two
+ * host threads, two contexts on one device) race on it. */
+int wg_logpdf_noalloc(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, double* total);
+
 /* Asynchronous pair for device-side timing: enqueue the evaluation on the
  * context stream (inputs already resident), then fetch the results (this
  * synchronises).  with_grad selects the adjoint. */

@@ -20,6 +20,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <string>
 
 #include "wg_internal.h"
 
@@ -1004,6 +1005,7 @@ struct SubBatch {
   double* d_gout = nullptr;
   double* d_gred = nullptr;
   int64_t gout_doubles = 0;
+  int64_t tops_doubles = 0;
   cudaStream_t s = nullptr, s2 = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, done = nullptr;
   ~SubBatch() {
@@ -1201,6 +1203,7 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
     sb->d_progs = dalloc<DProg2>(P.progs.size(), by);
     sb->d_lists = dalloc<int>(lists.size(), by);
     sb->d_tops = dalloc<double>(P.tops_doubles, by);
+    sb->tops_doubles = P.tops_doubles;
     if (keep) sb->d_tabs = dalloc<double>(P.tab_doubles, by);
     if (adjoint) {
       sb->d_bartops = dalloc<double>(P.tops_doubles, by);
@@ -1672,3 +1675,83 @@ int wg_fetch(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, double* 
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Forward evaluation that allocates nothing.
+//
+// Some callers cannot call cudaMalloc at the time they evaluate the
+// likelihood: hosts whose device memory is owned by another allocator or pool,
+// and sampler loops that must not enter the allocator between steps
+// (cudaMalloc can synchronise the device and can fail under memory pressure).
+// wg_logpdf allocates nothing per call either,
+// but its first call on a batch instantiates a CUDA graph, which does.  This
+// entry point runs the same forward task kernel with its scratch (the top
+// row of every task, read by the parent tasks) in the file-scope array below
+// instead of the batch's own buffer, and launches the levels directly.
+// ===========================================================================
+namespace {
+
+constexpr int64_t kNoAllocMaxTops = (int64_t)1 << 20;  // doubles (8 MiB), held by every device that loads the library
+__device__ __align__(256) double g_noalloc_tops[kNoAllocMaxTops];
+
+// Device address of g_noalloc_tops, looked up once per device (with that
+// device current) on the first call there.
+double* noalloc_scratch(int device) {
+  static std::mutex mu;
+  static double* addr[64] = {};
+  if (device < 0 || device >= 64) throw Error(WG_EINVAL, "device index out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[device]) {
+    void* p = nullptr;
+    ck(cudaGetSymbolAddress(&p, g_noalloc_tops), "cudaGetSymbolAddress(g_noalloc_tops)");
+    addr[device] = static_cast<double*>(p);
+  }
+  return addr[device];
+}
+
+}  // namespace
+
+extern "C" int wg_logpdf_noalloc(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, double* total) {
+  WG_GUARD({
+    if (!ctx || !m || !b || b->ctx != ctx) throw Error(WG_EINVAL, "wg_logpdf_noalloc: bad arguments");
+    check_model(b, m);
+    int64_t need = 0;
+    for (auto& sb : b->subs) need += sb->tops_doubles;
+    if (need > kNoAllocMaxTops)
+      throw Error(WG_ERANGE, "wg_logpdf_noalloc: the batch needs " + std::to_string(need) +
+                                 " doubles of scratch, more than the fixed " + std::to_string(kNoAllocMaxTops) +
+                                 " (split the families over smaller batches)");
+    ck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    double* scratch = noalloc_scratch(ctx->device);
+    cudaStream_t s = ctx->stream;
+    if (b->pending) ck(cudaStreamSynchronize(s), "pending evaluation");
+    const int NR = b->NR, K = b->K;
+    std::memcpy(b->h_params, m->eps.data(), NR * sizeof(double));
+    std::memcpy(b->h_params + NR, m->phi.data(), NR * sizeof(double));
+    std::memcpy(b->h_params + 2 * NR, m->psi.data(), NR * sizeof(double));
+    for (int k = 0; k < K; ++k) b->h_params[3 * NR + k] = std::isnan(m->q[k]) ? 0.0 : m->q[k];
+    b->h_params[3 * NR + K] = m->eta;
+    ck(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(double) * b->P, cudaMemcpyHostToDevice, s), "params upload");
+    // every top row is written by its task before a parent reads it, so the
+    // scratch needs no clearing; it keeps the last call's rows afterwards
+    int64_t off = 0;
+    for (auto& sbp : b->subs) {
+      SubBatch* sb = sbp.get();
+      KArgs2 A = sub_args(b, sb);
+      A.tops = scratch + off;
+      A.tabs = nullptr;
+      off += sb->tops_doubles;
+      for (int L = 0; L < (int)sb->lvl_n.size(); ++L) {
+        if (sb->lvlh_n[L] > 0)
+          k_fwd2<false, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], s>>>(A, sb->d_lists + sb->lvlh_off[L]);
+        if (sb->lvl_n[L] > 0)
+          k_fwd2<false, kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem[L], s>>>(A, sb->d_lists + sb->lvl_off[L]);
+      }
+    }
+    ck(cudaGetLastError(), "forward launch");
+    ck(cudaMemcpyAsync(b->h_logl, b->d_logl, sizeof(double) * b->NF, cudaMemcpyDeviceToHost, s), "logl download");
+    ck(cudaStreamSynchronize(s), "evaluation");
+    finish(m, b->NF, b->h_logl, nullptr, false, per_family, total, nullptr, nullptr, nullptr, nullptr, nullptr,
+           nullptr, nullptr);
+  });
+}
