@@ -253,6 +253,9 @@ def main():
     clk = clocks.stop()
     dev_step = float(np.mean(dev_ms))
     wall_step = wall / args.steps
+    nfw, ngr = W._native.C.c_int32(), W._native.C.c_int32()
+    W._native.check(L.wg_batch_launches(batch.h, W._native.C.byref(nfw), W._native.C.byref(ngr)))
+    n_launch = ngr.value
     if pg:
         t = torch.tensor([dev_step, wall_step], device=f"cuda:{local}", dtype=torch.float64)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
@@ -289,9 +292,9 @@ def main():
     # roofline of the dominant kernel (the adjoint or the forward)
     fa = float(np.mean(a_ms)), float(np.mean(f_ms))
     if fa[0] >= fa[1]:
-        kname, kms, kflops = "k_adjoint", fa[0], batch.flops_adj
+        kname, kms, kflops = "k_adj2 (all levels and size classes)", fa[0], batch.flops_adj
     else:
-        kname, kms, kflops = "k_forward<true>", fa[1], batch.flops_fwd
+        kname, kms, kflops = "k_fwd2<true> (all levels and size classes)", fa[1], batch.flops_fwd
     achieved = kflops / (kms * 1e-3) / 1e12
     roof = {"bound": "fp64", "kernel": kname, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
             "frac": achieved / fp64_peak if fp64_peak else None, "traffic": None,
@@ -315,7 +318,7 @@ def main():
                    "pack_seconds": pack_s},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": wall_step_ms},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": n_launch * args.steps,
         "kernel_ms": {"forward": float(np.mean(f_ms)), "adjoint": float(np.mean(a_ms)),
                       "reduce": float(np.mean(r_ms)), "forward_only": fwd_only_ms},
         "grad_cost_vs_forward": dev_step / fwd_only_ms,

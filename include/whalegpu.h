@@ -133,6 +133,11 @@ int wg_batch_destroy(wg_batch* b);
 int wg_batch_info(const wg_batch* b, int32_t* n_families, int32_t* n_groups, int64_t* device_bytes,
                   double* flops_fwd, double* bytes_fwd, double* flops_adj);
 
+/* Kernel launches in one evaluation of the batch as last recorded: forward
+ * only, and forward + adjoint + gradient reduction (0 before the first call
+ * of that kind).  Not in the reference (a measurement aid). */
+int wg_batch_launches(const wg_batch* b, int32_t* forward, int32_t* gradient);
+
 /* Pack a batch on the host only (no device needed) and report its layout:
  * tasks (CTAs over all launches), program entries, DP-table doubles kept for
  * the adjoint, largest shared memory per CTA (bytes) and the algorithmic

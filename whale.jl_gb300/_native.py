@@ -69,6 +69,7 @@ def _declare(L):
         "wg_pack_info": (C.c_int, [vp, P_vp, i32, u32, P_i64, P_i64, P_i64, P_i64, P_dbl]),
         "wg_pack_tasks": (C.c_int, [vp, P_vp, i32, u32, P_i32, i64, P_i64]),
         "wg_batch_info": (C.c_int, [vp, P_i32, P_i32, P_i64, P_dbl, P_dbl, P_dbl]),
+        "wg_batch_launches": (C.c_int, [vp, P_i32, P_i32]),
         "wg_logpdf": (C.c_int, [vp, vp, vp, P_dbl, P_dbl]),
         "wg_logpdf_grad": (C.c_int, [vp, vp, vp, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl]),
         "wg_logpdf_plain": (C.c_int, [vp, vp, vp, P_dbl, P_dbl]),

@@ -208,7 +208,7 @@ struct DTask {
   int32_t nfam = 0;     // families (root tasks: log L outputs)
   int32_t smem = 0;     // shared doubles needed (forward)
   int32_t nt = 0;       // threads of the CTA that runs the task
-  int32_t _pad2 = 0;
+  int32_t nslot_max = 0;  // partial slots of the largest program (shared-memory layout)
   int64_t tab = -1;     // DP table base, task-major [row][R] (-1: not kept)
   int64_t top = 0;      // top row base in the tops buffer
   int64_t gmap = 0;     // int64 per staged position (wa + wb): offset in tops

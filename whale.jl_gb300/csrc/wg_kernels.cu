@@ -255,6 +255,18 @@ __device__ __forceinline__ Raw decode(const ulonglong2 r) {
   return x;
 }
 
+// Asynchronous global -> shared copies (LDGSTS), 8 bytes per thread and
+// element, tracked in per-thread commit groups.
+__device__ __forceinline__ void cp_async8(double* dst, const double* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // General lane program: products accumulate, finalize ops call fin().
 template <class Fin>
 __device__ __forceinline__ void run_any(const DEntry* __restrict__ E, const DProg2& pr, int lane, const double* A,
@@ -291,11 +303,16 @@ __device__ __forceinline__ void run_comb(const DEntry* __restrict__ E, const DPr
 }
 
 // The same-row levels of the root (Πroot): level after level with a barrier
-// between them.  Levels are short, so the next level's descriptor and first
-// entries are loaded before the barrier that ends the current one.
-template <int NT, bool REVERSE = false, class Fin>
+// between them.  Entries are products or the finalize op FIN (entries with
+// f0 = f1 = c): v = fma(ψ, acc, ϕ·A[c]) handed to onfin(c, v, acc); like the
+// branch rows, both take one DMUL and one DFMA so warps never diverge on FP64.
+// Levels are short, so the next level's descriptor and first entries are
+// loaded before the barrier that ends the current one.  comb(opc, c, fa, fb, s)
+// finishes split clades after an extra barrier.
+template <int NT, bool REVERSE, unsigned FIN, class OnFin, class Comb>
 __device__ __forceinline__ void run_levels(const DEntry* __restrict__ E, const DProg2* __restrict__ progs, int nlvl,
-                                           int lane, const double* A, const double* B, double* part, Fin fin) {
+                                           int lane, const double* A, const double* B, double* part, double ph,
+                                           double ps, OnFin onfin, Comb comb) {
   if (nlvl <= 0) return;
   auto at = [&](int i) { return REVERSE ? nlvl - 1 - i : i; };
   DProg2 cur = progs[at(0)];
@@ -313,20 +330,23 @@ __device__ __forceinline__ void run_levels(const DEntry* __restrict__ E, const D
       double acc = 0.0;
       for (int j = 0; j < cur.J; ++j) {
         const Raw x = decode(j == 0 ? pre0 : (j == 1 ? pre1 : __ldg(e + (size_t)j * cur.nt)));
+        const bool fin = x.opc == FIN;
+        const double m = (fin ? ph : x.p) * A[x.f0];
+        const double v = fma(fin ? ps : m, fin ? acc : B[x.f1], fin ? m : acc);
         if (x.opc == op::PROD) {
-          acc = fma(x.p * A[x.f0], B[x.f1], acc);
+          acc = v;
+        } else if (fin) {
+          onfin(x.f0, v, acc);
+          acc = 0.0;
         } else if (x.opc == op::FIN_PART) {
           part[x.f2] = acc;
-          acc = 0.0;
-        } else if (x.opc != op::NOP) {
-          fin(x.opc, x.f0, x.f1, x.f2, acc);
           acc = 0.0;
         }
       }
     }
     if (cur.ncomb) {
       __syncthreads();
-      run_comb<NT>(E, cur, part, fin);
+      run_comb<NT>(E, cur, part, comb);
     }
     if (i + 1 < nlvl) {
       pre0 = pre1 = make_ulonglong2(0, (uint64_t)op::NOP << 48);
@@ -432,6 +452,83 @@ __device__ __forceinline__ double eps_top2(const KArgs2& A, int k) {
   return A.params[A.row_off[k] + A.mnode[k].w - 1];
 }
 
+// Rows 1..n-1 of a branch with the lane program in registers, J exact (no
+// guarded iterations).  cur/nxt are swapped row by row.
+template <int NT, bool TABLES, int J>
+__device__ __forceinline__ void fwd_rows(const DEntry* __restrict__ E, const DTask& T, int lane, int n, int R,
+                                         const double* phs, const double* pss, double*& cur, double*& nxt,
+                                         double* part, double* tab0) {
+  const DProg2 dup = T.dup;  // held in registers: the rows store to global memory
+  LaneProg<J> lp;
+  load_lane_prog<J>(E, dup, lane, lp);
+  const bool active = lane < dup.nt;
+  for (int r = 1; r < n; ++r) {
+    const double ph = phs[r], ps = pss[r];
+    double* tr = TABLES ? tab0 + (int64_t)r * R : nullptr;
+    double* o = nxt;
+    if (active)
+      rows_reg<J, op::FIN_DUP>(lp, cur, cur, part, ph, ps, [&](unsigned c, double v, double) {
+        o[c] = v;
+        if (TABLES) tr[c] = v;
+      });
+    if (dup.ncomb) {
+      __syncthreads();
+      const double* cc = cur;
+      run_comb<NT>(E, dup, part, [&](unsigned, unsigned c, unsigned, unsigned, double s) {
+        const double v = fma(ps, s, ph * cc[c]);
+        o[c] = v;
+        if (TABLES) tr[c] = v;
+      });
+    }
+    __syncthreads();
+    double* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+}
+
+template <int NT, bool TABLES>
+__device__ __forceinline__ void fwd_rows_generic(const DEntry* __restrict__ E, const DTask& T, int lane, int n, int R,
+                                                 const double* phs, const double* pss, double*& cur, double*& nxt,
+                                                 double* part, double* tab0) {
+  const DProg2 dup = T.dup;
+  for (int r = 1; r < n; ++r) {
+    const double ph = phs[r], ps = pss[r];
+    double* tr = TABLES ? tab0 + (int64_t)r * R : nullptr;
+    run_rows<TABLES>(E, dup, lane, cur, nxt, part, ph, ps, tr);
+    if (dup.ncomb) {
+      __syncthreads();
+      const double* cc = cur;
+      double* o = nxt;
+      run_comb<NT>(E, dup, part, [&](unsigned, unsigned c, unsigned, unsigned, double s) {
+        const double v = fma(ps, s, ph * cc[c]);
+        o[c] = v;
+        if (TABLES) tr[c] = v;
+      });
+    }
+    __syncthreads();
+    double* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+}
+
+template <int NT, bool TABLES, int J = 1>
+__device__ __forceinline__ bool fwd_rows_dispatch(int j, const DEntry* __restrict__ E, const DTask& T, int lane, int n,
+                                                  int R, const double* phs, const double* pss, double*& cur,
+                                                  double*& nxt, double* part, double* tab0) {
+  constexpr int MAXJ = NT == kNT2L ? 8 : 12;
+  if constexpr (J > MAXJ) {
+    return false;
+  } else {
+    if (j == J) {
+      fwd_rows<NT, TABLES, J>(E, T, lane, n, R, phs, pss, cur, nxt, part, tab0);
+      return true;
+    }
+    return fwd_rows_dispatch<NT, TABLES, J + 1>(j, E, T, lane, n, R, phs, pss, cur, nxt, part, tab0);
+  }
+}
+
 template <bool TABLES, int NT>
 __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restrict__ list) {
   extern __shared__ double sm[];
@@ -491,45 +588,26 @@ __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restri
         const double xi = 1.0 - (1.0 - eta) * er;
         const double ca = (1.0 - eta) * xi / eta;
         const double cb = eta * (1.0 - er) / (xi * xi);
-        auto lfin = [&](unsigned, unsigned c, unsigned, unsigned, double acc) { cur[c] = fma(ca, acc, cb * cur[c]); };
-        run_levels<NT>(E, A.progs + T.lvl, T.nlvl, lane, cur, cur, part, lfin);
+        auto lcomb = [&](unsigned, unsigned c, unsigned, unsigned, double acc) { cur[c] = fma(ca, acc, cb * cur[c]); };
+        run_levels<NT, false, op::FIN_LVL>(E, A.progs + T.lvl, T.nlvl, lane, cur, cur, part, cb, ca,
+                                           [&](unsigned c, double v, double) { cur[c] = v; }, lcomb);
       }
     }
   }
   __syncthreads();
   if (TABLES)
     for (int c = tid; c < R; c += NT) A.tabs[T.tab + c] = cur[c];
-  if (mn.x != WG_NODE_ROOT) {
-    constexpr int MAXJ = NT == kNT2L ? 8 : 16;
-    LaneProg<MAXJ> lp;
-    const bool inreg = T.dup.J <= MAXJ;
-    if (inreg) load_lane_prog<MAXJ>(E, T.dup, lane, lp);
-    for (int r = 1; r < mn.w; ++r) {
-      const double ph = A.params[NR + roff + r], ps = A.params[2 * NR + roff + r];
-      double* tr = TABLES ? A.tabs + T.tab + (int64_t)r * R : nullptr;
-      if (inreg) {
-        double* o = nxt;
-        rows_reg<MAXJ, op::FIN_DUP>(lp, cur, cur, part, ph, ps, [&](unsigned c, double v, double) {
-          o[c] = v;
-          if (TABLES) tr[c] = v;
-        });
-      } else {
-        run_rows<TABLES>(E, T.dup, lane, cur, nxt, part, ph, ps, tr);
-      }
-      if (T.dup.ncomb) {
-        __syncthreads();
-        auto cfin = [&](unsigned, unsigned c, unsigned, unsigned, double s) {
-          const double v = fma(ps, s, ph * cur[c]);
-          nxt[c] = v;
-          if (TABLES) tr[c] = v;
-        };
-        run_comb<NT>(E, T.dup, part, cfin);
-      }
-      __syncthreads();
-      double* t = cur;
-      cur = nxt;
-      nxt = t;
+  if (mn.x != WG_NODE_ROOT && mn.w > 1) {
+    double* phs = part + T.nslot_max;  // ϕ, ψ of this branch's rows
+    double* pss = phs + mn.w;
+    for (int r = tid; r < mn.w; r += NT) {
+      phs[r] = A.params[NR + roff + r];
+      pss[r] = A.params[2 * NR + roff + r];
     }
+    __syncthreads();
+    double* tab0 = TABLES ? A.tabs + T.tab : nullptr;
+    if (!fwd_rows_dispatch<NT, TABLES>(T.dup.J, E, T, lane, mn.w, R, phs, pss, cur, nxt, part, tab0))
+      fwd_rows_generic<NT, TABLES>(E, T, lane, mn.w, R, phs, pss, cur, nxt, part, tab0);
   }
   double* top = A.tops + T.top;
   for (int c = tid; c < R; c += NT) top[c] = cur[c];
@@ -603,6 +681,133 @@ __device__ __forceinline__ void block_sum4(double (&v)[4], double* red) {
 // Reverse sweep of one task.  Per-task outputs (gout + T.gout):
 // [2r] ∂/∂ϕ_r, [2r+1] ∂/∂ψ_r (rows r >= 1), [2n] ∂/∂ε_top(child 0),
 // [2n+1] ∂/∂ε_top(child 1), [2n+2] ∂/∂q, [2n+3] ∂/∂η, [2n+4] ∂/∂ε_top(own).
+// Reverse rows n-1 .. 1 of a branch.  J > 0: lane program in registers with
+// exactly J iterations; J == 0: entries streamed from memory.  Per row:
+// G[x] = Σ p·bar[γ]·L[sib], bar_{r-1}[x] = ϕ bar[x] + ψ G[x]; then
+// ∂/∂ϕ_r = Σ bar_r·L_{r-1} and ∂/∂ψ_r = ½ Σ G·L_{r-1} (each split counted
+// twice) in a full-lane dot loop, reduced 8 rows at a time by a register-ring
+// reduce-scatter.
+template <int NT, int J>
+__device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTask& T, int lane, int n, int R,
+                                         const double* phs, const double* pss, double*& bar, double*& barn,
+                                         double* Lb, int W2, double* Gs, double* part, double* red,
+                                         const double* tab0, double* out) {
+  const int tid = threadIdx.x, wid = tid >> 5, wl = tid & 31;
+  double rp[8], rs[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) rp[i] = rs[i] = 0.0;
+  const DProg2 td = T.tdup;  // held in registers: the loop stores to global memory
+  LaneProg<(J > 0 ? J : 1)> lp;
+  if (J > 0) load_lane_prog<(J > 0 ? J : 1)>(E, td, lane, lp);
+  const bool active = lane < td.nt;
+  // Row r reads table row r-1 from buffer (n-1-r) mod 3 (buffer i at Lb +
+  // i·W2); the copies run two rows ahead, one commit group per row (empty
+  // past row 1).
+  auto fetch = [&](int rr, double* dst) {
+    if (rr >= 1) {
+      const double* src = tab0 + (int64_t)(rr - 1) * R;
+      for (int c = tid; c < R; c += NT) cp_async8(dst + c, src + c);
+    }
+    cp_async_commit();
+  };
+  fetch(n - 1, Lb);
+  fetch(n - 2, Lb + W2);
+  int bi = 0;
+  for (int r = n - 1; r >= 1; --r) {
+    double* Lp = Lb + bi * W2;
+    cp_async_wait<1>();
+    __syncthreads();
+    // every thread is past row r+1, whose buffer takes table row r-3
+    fetch(r - 2, Lb + (bi == 0 ? 2 : bi - 1) * W2);
+    bi = bi == 2 ? 0 : bi + 1;
+    const double ph = phs[r], ps = pss[r];
+    double* bn = barn;
+    const double* bb = bar;
+    if (J > 0) {
+      if (active)
+        rows_reg<(J > 0 ? J : 1), op::FIN_ADJ>(lp, bb, Lp, part, ph, ps, [&](unsigned c, double v, double g) {
+          bn[c] = v;
+          Gs[c] = g;
+        });
+    } else if (active) {
+      const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + td.off) + lane;
+      double acc = 0.0;
+      for (int j = 0; j < td.J; ++j, e += td.nt) {
+        const Raw x = decode(__ldg(e));
+        const bool fin = x.opc == op::FIN_ADJ;
+        const double m = (fin ? ph : x.p) * bb[x.f0];
+        const double v = fma(fin ? ps : m, fin ? acc : Lp[x.f1], fin ? m : acc);
+        if (x.opc == op::PROD) {
+          acc = v;
+        } else if (fin) {
+          bn[x.f0] = v;
+          Gs[x.f0] = acc;
+          acc = 0.0;
+        } else if (x.opc == op::FIN_PART) {
+          part[x.f2] = acc;
+          acc = 0.0;
+        }
+      }
+    }
+    if (td.ncomb) {
+      __syncthreads();
+      run_comb<NT>(E, td, part, [&](unsigned, unsigned c, unsigned, unsigned, double g) {
+        bn[c] = fma(ps, g, ph * bb[c]);
+        Gs[c] = g;
+      });
+    }
+    __syncthreads();
+    double dphi = 0.0, dpsi = 0.0;
+    for (int c = tid; c < R; c += NT) {
+      const double l = Lp[c];
+      dphi = fma(bb[c], l, dphi);
+      dpsi = fma(Gs[c], l, dpsi);
+    }
+    const int slot = (n - 1 - r) & 7;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      rp[i] = (i == slot) ? dphi : rp[i];
+      rs[i] = (i == slot) ? dpsi : rs[i];
+    }
+    if (slot == 7 || r == 1) {
+      int idx;
+      const double v = reduce_scatter16(rp, rs, wl, idx);
+      if ((wl & 1) == 0) red[16 * wid + idx] = v;
+      __syncthreads();
+      if (tid < 16) {
+        double sum = 0.0;
+        for (int q = 0; q < NT / 32; ++q) sum += red[16 * q + tid];
+        const int i = tid & 7;
+        const int rr = r + slot - i;  // row of batch slot i
+        if (i <= slot) out[2 * rr + (tid >> 3)] = (tid >> 3) ? 0.5 * sum : sum;
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i) rp[i] = rs[i] = 0.0;
+    }
+    double* t = bar;
+    bar = barn;
+    barn = t;
+  }
+  cp_async_wait<0>();  // only empty groups remain; row 0 reuses the buffers
+}
+
+template <int NT, int J = 1>
+__device__ __forceinline__ bool adj_rows_dispatch(int j, const DEntry* __restrict__ E, const DTask& T, int lane, int n,
+                                                  int R, const double* phs, const double* pss, double*& bar,
+                                                  double*& barn, double* Lb, int W2, double* Gs, double* part,
+                                                  double* red, const double* tab0, double* out) {
+  constexpr int MAXJ = NT == kNT2L ? 8 : 12;
+  if constexpr (J > MAXJ) {
+    return false;
+  } else {
+    if (j == J) {
+      adj_rows<NT, J>(E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out);
+      return true;
+    }
+    return adj_rows_dispatch<NT, J + 1>(j, E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out);
+  }
+}
+
 template <int NT>
 __global__ void __launch_bounds__(NT, NT == 128 ? 6 : 2) k_adj2(const KArgs2 A, const int* __restrict__ list) {
   extern __shared__ double sm[];
@@ -618,10 +823,10 @@ __global__ void __launch_bounds__(NT, NT == 128 ? 6 : 2) k_adj2(const KArgs2 A, 
   const int n = mn.w;
   double* bar = sm;
   double* barn = sm + W2;
-  double* L0 = sm + 2 * W2;
+  double* L0 = sm + 2 * W2;  // L0, L1 and a third buffer: table rows of the branch
   double* L1 = sm + 3 * W2;
-  double* Gs = sm + 4 * W2;
-  double* part = sm + 5 * W2;
+  double* Gs = sm + 5 * W2;
+  double* part = sm + 6 * W2;
   int ms = max(max(T.tdup.nslot, T.ta.nslot), max(T.tb.nslot, T.init.nslot));
   for (int q = 0; q < T.nlvl; ++q) ms = max(ms, A.progs[T.tlvl + q].nslot);
   double* red = part + ms;  // 16 * warps doubles
@@ -647,11 +852,20 @@ __global__ void __launch_bounds__(NT, NT == 128 ? 6 : 2) k_adj2(const KArgs2 A, 
     const double ca = (1.0 - eta) * xi / eta;
     const double cb = eta * (1.0 - er) / (xi * xi);
     double acc4[4] = {0.0, 0.0, 0.0, 0.0};  // dca, dcb, dea, deb
-    auto tfin = [&](unsigned, unsigned c, unsigned, unsigned, double g) {
-      bar[c] += ca * g;
-      acc4[0] += 0.5 * g * L0[c];
+    for (int c = tid; c < R; c += NT) Gs[c] = 0.0;
+    __syncthreads();
+    auto tcomb = [&](unsigned, unsigned c, unsigned, unsigned, double g) {
+      bar[c] = fma(ca, g, bar[c]);
+      Gs[c] = g;
     };
-    run_levels<NT, true>(E, A.progs + T.tlvl, T.nlvl, lane, bar, L0, part, tfin);
+    run_levels<NT, true, op::FIN_TLVL>(E, A.progs + T.tlvl, T.nlvl, lane, bar, L0, part, 1.0, ca,
+                                       [&](unsigned c, double v, double g) {
+                                         bar[c] = v;
+                                         Gs[c] = g;
+                                       },
+                                       tcomb);
+    // ∂/∂ca = Σ bar[γ]·Πroot(γ) = ½ Σ_x G[x]·L[x] (each split counted twice)
+    for (int c = tid; c < R; c += NT) acc4[0] += 0.5 * Gs[c] * L0[c];
     // stage the children's tops, recompute Πspec + Πloss for ∂/∂cb
     double* X = barn;
     double* Y = barn + T.wa;
@@ -713,87 +927,17 @@ __global__ void __launch_bounds__(NT, NT == 128 ? 6 : 2) k_adj2(const KArgs2 A, 
   }
   // ---- rows n-1 .. 1 of the branch (within_branch!)
   for (int c = tid; c < R; c += NT) bar[c] = A.bartops[T.top + c];
-  double rp[8], rs[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) rp[i] = rs[i] = 0.0;
-  const int wid = tid >> 5, wl = tid & 31;
-  constexpr int MAXJ = NT == kNT2L ? 8 : 16;
-  LaneProg<MAXJ> lp;
-  const bool inreg = T.tdup.J <= MAXJ && n > 1;
-  if (inreg) load_lane_prog<MAXJ>(E, T.tdup, lane, lp);
-  for (int r = n - 1; r >= 1; --r) {
-    double* Lp = ((n - 1 - r) & 1) ? L1 : L0;
-    const double* lr = A.tabs + T.tab + (int64_t)(r - 1) * R;
-    for (int c = tid; c < R; c += NT) Lp[c] = lr[c];
-    __syncthreads();
-    const double ph = A.params[NR + roff + r], ps = A.params[2 * NR + roff + r];
-    // products G[x] = Σ p·bar[γ]·L[sib] and bar_{r-1}[x] = ϕ bar[x] + ψ G[x]
-    if (inreg) {
-      double* bn = barn;
-      rows_reg<MAXJ, op::FIN_ADJ>(lp, bar, Lp, part, ph, ps, [&](unsigned c, double v, double g) {
-        bn[c] = v;
-        Gs[c] = g;
-      });
-    } else if (lane < T.tdup.nt) {
-      const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + T.tdup.off) + lane;
-      double acc = 0.0;
-      for (int j = 0; j < T.tdup.J; ++j, e += T.tdup.nt) {
-        const Raw x = decode(__ldg(e));
-        const bool fin = x.opc == op::FIN_ADJ;
-        const double m = (fin ? ph : x.p) * bar[x.f0];
-        const double v = fma(fin ? ps : m, fin ? acc : Lp[x.f1], fin ? m : acc);
-        if (x.opc == op::PROD) {
-          acc = v;
-        } else if (fin) {
-          barn[x.f0] = v;
-          Gs[x.f0] = acc;
-          acc = 0.0;
-        } else if (x.opc == op::FIN_PART) {
-          part[x.f2] = acc;
-          acc = 0.0;
-        }
-      }
-    }
-    if (T.tdup.ncomb) {
-      __syncthreads();
-      auto cfin = [&](unsigned, unsigned c, unsigned, unsigned, double g) {
-        barn[c] = fma(ps, g, ph * bar[c]);
-        Gs[c] = g;
-      };
-      run_comb<NT>(E, T.tdup, part, cfin);
+  if (n > 1) {
+    double* phs = red + 16 * (NT / 32);  // ϕ, ψ of this branch's rows
+    double* pss = phs + n;
+    for (int r = tid; r < n; r += NT) {
+      phs[r] = A.params[NR + roff + r];
+      pss[r] = A.params[2 * NR + roff + r];
     }
     __syncthreads();
-    // ∂/∂ϕ_r = Σ bar_r·L_{r-1}, ∂/∂ψ_r = ½ Σ G·L_{r-1} (each split counted twice)
-    double dphi = 0.0, dpsi = 0.0;
-    for (int c = tid; c < R; c += NT) {
-      const double l = Lp[c];
-      dphi = fma(bar[c], l, dphi);
-      dpsi = fma(Gs[c], l, dpsi);
-    }
-    const int slot = (n - 1 - r) & 7;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      rp[i] = (i == slot) ? dphi : rp[i];
-      rs[i] = (i == slot) ? dpsi : rs[i];
-    }
-    if (slot == 7 || r == 1) {
-      int idx;
-      const double v = reduce_scatter16(rp, rs, wl, idx);
-      if ((wl & 1) == 0) red[16 * wid + idx] = v;
-      __syncthreads();
-      if (tid < 16) {
-        double s = 0.0;
-        for (int q = 0; q < NT / 32; ++q) s += red[16 * q + tid];
-        const int i = tid & 7;
-        const int rr = r + slot - i;  // row of batch slot i
-        if (i <= slot) out[2 * rr + (tid >> 3)] = (tid >> 3) ? 0.5 * s : s;
-      }
-#pragma unroll
-      for (int i = 0; i < 8; ++i) rp[i] = rs[i] = 0.0;
-    }
-    double* t = bar;
-    bar = barn;
-    barn = t;
+    const double* tab0 = A.tabs + T.tab;
+    if (!adj_rows_dispatch<NT>(T.tdup.J, E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red, tab0, out))
+      adj_rows<NT, 0>(E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red, tab0, out);
   }
   __syncthreads();
   // ---- row 0
@@ -1038,6 +1182,7 @@ struct wg_batch {
   double* h_gred = nullptr;  // P per sub-batch
   bool grad_pending = false;
   bool pending = false;  // an enqueued evaluation has not been fetched yet
+  int launches[2] = {0, 0};  // kernels per recorded sequence: [forward only, with gradient]
   std::vector<wg_ccd*> ccds;  // not owned; for the lazily built plain layout
   std::unique_ptr<PlainBatch> plain;
   // captured launch sequences: [with gradient][with tables]
@@ -1131,7 +1276,11 @@ KArgs plain_args(const PlainBatch* b) {
 }
 
 // Size classes by clade count (upper bounds); one layout per non-empty class.
-constexpr int kClassBounds[] = {256, 1024, 1 << 30};
+// Families are split by clade count into size classes, each packed on its
+// own and run on its own pair of streams: the levels of one class do not wait
+// for the levels of another.  Larger classes carry the critical paths and get
+// higher stream priorities, so their CTAs are dispatched first.
+constexpr int kClassBounds[] = {128, 256, 512, 1024, 1536, 1 << 30};
 
 std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* const* ccds, int n, uint32_t flags) {
   ck(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -1152,7 +1301,11 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
   const bool adjoint = (flags & WG_BATCH_GRAD) != 0;
   const bool keep = (flags & (WG_BATCH_GRAD | WG_BATCH_TABLES)) != 0;
   int lo = 0;
+  int prio_lo = 0, prio_hi = 0;
+  ck(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi), "priority range");
+  int cls = -1;
   for (int bound : kClassBounds) {
+    ++cls;
     std::vector<int> ids;
     for (int i = 0; i < n; ++i)
       if (ccds[i]->n_clades > lo && ccds[i]->n_clades <= bound) ids.push_back(i);
@@ -1221,8 +1374,12 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
     h2d(sb->d_gmap, P.gmap, s);
     h2d(sb->d_progs, P.progs, s);
     h2d(sb->d_lists, lists, s);
-    ck(cudaStreamCreateWithFlags(&sb->s, cudaStreamNonBlocking), "cudaStreamCreate");
-    ck(cudaStreamCreateWithFlags(&sb->s2, cudaStreamNonBlocking), "cudaStreamCreate");
+    {
+      // priority grows (numerically falls) with the class
+      const int pr = std::max(prio_hi, prio_lo - cls);
+      ck(cudaStreamCreateWithPriority(&sb->s, cudaStreamNonBlocking, pr), "cudaStreamCreate");
+      ck(cudaStreamCreateWithPriority(&sb->s2, cudaStreamNonBlocking, pr), "cudaStreamCreate");
+    }
     for (cudaEvent_t* e : {&sb->fork, &sb->join, &sb->done})
       ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
     b->subs.push_back(std::move(sb));
@@ -1303,6 +1460,8 @@ void join_subs(wg_batch* b) {
 void record_sequence(wg_batch* b, bool grad, bool tables) {
   wg_ctx* ctx = b->ctx;
   cudaStream_t s = ctx->stream;
+  int& nl = b->launches[grad ? 1 : 0];
+  nl = 0;
   ck(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(double) * b->P, cudaMemcpyHostToDevice, s), "params upload");
   if (grad)
     for (auto& sb : b->subs)
@@ -1318,10 +1477,12 @@ void record_sequence(wg_batch* b, bool grad, bool tables) {
       run_level(
           sb, L,
           [&](cudaStream_t st) {
+            ++nl;
             if (tables) k_fwd2<true, kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem[L], st>>>(A, ll);
             else k_fwd2<false, kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem[L], st>>>(A, ll);
           },
           [&](cudaStream_t st) {
+            ++nl;
             if (tables) k_fwd2<true, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], st>>>(A, lh);
             else k_fwd2<false, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], st>>>(A, lh);
           });
@@ -1339,9 +1500,17 @@ void record_sequence(wg_batch* b, bool grad, bool tables) {
         const int* ll = sb->d_lists + sb->lvl_off[L];
         const int* lh = sb->d_lists + sb->lvlh_off[L];
         run_level(
-            sb, L, [&](cudaStream_t st) { k_adj2<kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem_adj[L], st>>>(A, ll); },
-            [&](cudaStream_t st) { k_adj2<kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem_adj[L], st>>>(A, lh); });
+            sb, L,
+            [&](cudaStream_t st) {
+              ++nl;
+              k_adj2<kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem_adj[L], st>>>(A, ll);
+            },
+            [&](cudaStream_t st) {
+              ++nl;
+              k_adj2<kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem_adj[L], st>>>(A, lh);
+            });
       }
+      ++nl;
       k_reduce2<<<(b->P * 32 + 255) / 256, 256, 0, sb->s>>>(sb->d_gout, sb->d_red_off, sb->d_red_idx, b->P,
                                                             sb->d_gred);
     }
@@ -1384,7 +1553,8 @@ void enqueue(wg_batch* b, const wg_model* m, bool grad) {
     }
     cudaGraph_t g = nullptr;
     ck(cudaStreamEndCapture(s, &g), "end capture");
-    const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+    // kernel nodes keep the priorities of the streams they were captured on
+    const cudaError_t e = cudaGraphInstantiate(&ge, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     ck(e, "graph instantiate");
   }
@@ -1586,6 +1756,14 @@ int wg_batch_info(const wg_batch* b, int32_t* n_families, int32_t* n_groups, int
     if (flops_fwd) *flops_fwd = b->flops_fwd;
     if (bytes_fwd) *bytes_fwd = b->bytes_fwd;
     if (flops_adj) *flops_adj = b->flops_adj;
+  });
+}
+
+int wg_batch_launches(const wg_batch* b, int32_t* forward, int32_t* gradient) {
+  WG_GUARD({
+    if (!b) throw Error(WG_EINVAL, "null batch");
+    if (forward) *forward = b->launches[0];
+    if (gradient) *gradient = b->launches[1];
   });
 }
 

@@ -892,7 +892,10 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
           for (int g = 0; g < c.n_clades; ++g) plevel[pos(i, g)] = lvl[fams[i]][g];
         }
         std::vector<Item> tby;
-        if (opt.adjoint) { tby.resize(R); for (int x = 0; x < R; ++x) { tby[x].c = x; tby[x].fin = op::FIN_TLVL; } }
+        if (opt.adjoint) {
+          tby.resize(R);
+          for (int x = 0; x < R; ++x) { tby[x].c = x; tby[x].fin = op::FIN_TLVL; tby[x].fa = x; tby[x].fb = x; }
+        }
         for (int i = 0; i < nf; ++i) {
           const CCD& c = *ccds[fams[i]];
           for (int g = 0; g < c.n_clades; ++g) {
@@ -900,6 +903,8 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
             Item it;
             it.c = pg;
             it.fin = op::FIN_LVL;
+            it.fa = pg;
+            it.fb = pg;
             if (c.nleaves[g] > 1)
               for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s) {
                 const int a = pos(i, c.g1[s]), b = pos(i, c.g2[s]);
@@ -929,8 +934,10 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       // forward: cur, nxt (children staged in nxt); adjoint: bar, barn, two
       // L rows, G; then partial slots and reduction scratch
       const int W2 = std::max(R, T.wa + T.wb);
-      T.smem = 2 * W2 + slots + 16 * (NT / 32) + 32;
-      const int smem_adj = 5 * W2 + slots + 16 * (NT / 32) + 32;
+      T.nslot_max = slots;
+      // + the branch's ϕ and ψ rows staged in shared memory
+      T.smem = 2 * W2 + slots + 2 * m.nrow[k] + 16 * (NT / 32) + 32;
+      const int smem_adj = 6 * W2 + slots + 2 * m.nrow[k] + 16 * (NT / 32) + 32;
       if (opt.adjoint) {
         T.gout = P.gout_doubles;
         const int n = m.nrow[k];
