@@ -100,6 +100,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# DRAM bytes per evaluation of the 5,000-family workload, summed over the
+# launches of each kernel family, from the ncu launch list kept in
+# profiles/launches_cfg1_5000fam.txt (not measurable inside the timed run).
+NCU_DRAM_BYTES = {"adjoint": 777_427_712, "forward": 370_898_432}
+
+
+def workload(nf):
+    return (f"cfg1: {nf:,} families, 17-taxon Yule tree + 3 WGDs, Δt=0.02, DLWGD log-normal rates; "
+            "log-likelihood + gradient (70 parameters) per step")
+
+
 def perturbed(W, wm, rng, scale=0.01):
     r = wm.rates
     return wm(W.DLWGD(λ=r.λ + rng.normal(0, scale, r.λ.size), μ=r.μ + rng.normal(0, scale, r.μ.size), q=r.q,
@@ -157,15 +168,16 @@ def run_reference(args, W, rank):
 
     wl = synth.config1(n_families=args.families)
     threads = os.cpu_count() or 1
-    idx = pick_cpu_sample(W, wl, args.cpu_budget / max(1, args.steps + args.warmup), threads)
+    # each step a bounded sample, large enough to keep every host thread busy
+    idx = pick_cpu_sample(W, wl, max(0.5, args.cpu_budget / max(1, args.steps + args.warmup)), threads)
     v, times = cpu_reference(W, wl, idx, args.steps, args.warmup, threads)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "cfg1 sample: 17-taxon Yule + 3 WGDs, Δt=0.02, DLWGD rates; logL + gradient "
-                               "(70 parameters) by forward-mode duals of chunk 12",
-                   "families_in_sample": len(idx), "families_in_workload": args.families},
+        "config": {"workload": workload(args.families), "families": args.families,
+                   "families_in_sample": len(idx),
+                   "method": "logL + gradient by forward-mode duals of chunk 12 on host cores"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{len(idx)} of {args.families} families (random, seed 7) per step"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -178,7 +190,7 @@ def run_reference(args, W, rank):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--families", type=int, default=5000)
@@ -293,11 +305,15 @@ def main():
     fa = float(np.mean(a_ms)), float(np.mean(f_ms))
     if fa[0] >= fa[1]:
         kname, kms, kflops = "k_adj2 (all levels and size classes)", fa[0], batch.flops_adj
+        traffic = NCU_DRAM_BYTES["adjoint"] if NF == 5000 else None
     else:
         kname, kms, kflops = "k_fwd2<true> (all levels and size classes)", fa[1], batch.flops_fwd
+        traffic = NCU_DRAM_BYTES["forward"] if NF == 5000 else None
     achieved = kflops / (kms * 1e-3) / 1e12
     roof = {"bound": "fp64", "kernel": kname, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-            "frac": achieved / fp64_peak if fp64_peak else None, "traffic": None,
+            "frac": achieved / fp64_peak if fp64_peak else None, "traffic": traffic,
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum over the kernel's launches of one "
+                              "evaluation, one ncu capture of this workload (profiles/launches_cfg1_5000fam.txt)",
             "peak_source": "measured in this run: register-resident DFMA loop (wg_probe_fp64); "
                            "MEASURED_PEAKS.json has no FP64 figure",
             "algorithmic_flops_per_launch": kflops, "launch_ms": kms,
@@ -306,8 +322,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "cfg1: 5,000 families, 17-taxon Yule + 3 WGDs, Δt=0.02, DLWGD log-normal rates, "
-                               "batched forward + adjoint (70 parameters)",
+        "config": {"workload": workload(NF),
                    "families": NF, "clades_mean": float(np.mean([c.n_clades for c in ccds])),
                    "clades_max": int(max(c.n_clades for c in ccds)),
                    "triples_mean": float(np.mean([c.n_triples for c in ccds])), "slices": NR,

@@ -252,7 +252,7 @@ constexpr int kNT2L = 128;   // threads per CTA of light tasks
 constexpr int kNT2H = 256;   // threads per CTA of heavy (single large family) tasks
 
 struct PackOptions2 {
-  int64_t target_ops = 320;   // forward product + finalize ops per row per task
+  int64_t target_ops = 480;   // forward product + finalize ops per row per task
   int64_t heavy_ops = 1024;   // non-root tasks above this many ops per row get kNT2H threads
   int64_t max_width = 6144;   // cap on a task's row width
   int target_j = 3;           // iterations per row the lane scheduler aims for

@@ -42,7 +42,7 @@ struct KArgs {
   const int4* mnode;     // kind, child0, child1, nrow
   const int* row_off;    // K + 1
   const double* leafp;   // K
-  const double* params;  // eps | phi | psi (NR each) | q (K) | eta
+  const double* params;  // eps | phi | psi (NR each) | q (K) | eta | ca | cb
   double* tops;
   double* tabs;
   double* bartops;
@@ -231,7 +231,7 @@ struct KArgs2 {
   const int4* mnode;     // kind, child0, child1, nrow
   const int* row_off;
   const double* leafp;
-  const double* params;  // eps | phi | psi (NR each) | q (K) | eta
+  const double* params;  // eps | phi | psi (NR each) | q (K) | eta | ca | cb
   double* tops;
   double* tabs;
   double* bartops;
@@ -267,98 +267,86 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// L1 prefetch of a lane's entries of a program (and of the thread's first
+// combine entry), issued at task start so that the phases that read them
+// later do not each wait a full memory latency.
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void prefetch_prog(const DEntry* __restrict__ E, const DProg2& pr, int lane) {
+  if (lane < pr.nt)
+    for (int j = 0; j < pr.J; ++j) prefetch_l1(E + pr.off + (size_t)j * pr.nt + lane);
+  if ((int)threadIdx.x < pr.ncomb) prefetch_l1(E + pr.comb + threadIdx.x);
+}
+
 // General lane program: products accumulate, finalize ops call fin().
+// Entries are fetched four at a time ahead of their use.
 template <class Fin>
 __device__ __forceinline__ void run_any(const DEntry* __restrict__ E, const DProg2& pr, int lane, const double* A,
                                         const double* B, double* part, Fin fin) {
   if (lane >= pr.nt) return;
   const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + pr.off) + lane;
+  const ulonglong2 nop = make_ulonglong2(0, (uint64_t)op::NOP << 48);
   double acc = 0.0;
-  for (int j = 0; j < pr.J; ++j, e += pr.nt) {
-    const Raw x = decode(__ldg(e));
-    if (x.opc == op::PROD) {
-      acc = fma(x.p * A[x.f0], B[x.f1], acc);
-    } else if (x.opc == op::FIN_PART) {
-      part[x.f2] = acc;
-      acc = 0.0;
-    } else if (x.opc != op::NOP) {
-      fin(x.opc, x.f0, x.f1, x.f2, acc);
-      acc = 0.0;
+  for (int j0 = 0; j0 < pr.J; j0 += 4) {
+    ulonglong2 r[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) r[u] = j0 + u < pr.J ? __ldg(e + (size_t)(j0 + u) * pr.nt) : nop;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const Raw x = decode(r[u]);
+      if (x.opc == op::PROD) {
+        acc = fma(x.p * A[x.f0], B[x.f1], acc);
+      } else if (x.opc == op::FIN_PART) {
+        part[x.f2] = acc;
+        acc = 0.0;
+      } else if (x.opc != op::NOP) {
+        fin(x.opc, x.f0, x.f1, x.f2, acc);
+        acc = 0.0;
+      }
     }
   }
+}
+
+// One combine entry: the partial sums of a split clade (two interleaved
+// chains), handed to fin().
+template <class Fin>
+__device__ __forceinline__ void comb_one(const ulonglong2 raw, const double* part, Fin fin) {
+  const Raw x = decode(raw);
+  const unsigned s0 = (unsigned)(raw.y & 0xFFFFFFFFu), n = (unsigned)(raw.y >> 32);
+  double s = part[s0], t = 0.0;
+  unsigned k = 1;
+  for (; k + 1 < n; k += 2) {
+    s += part[s0 + k];
+    t += part[s0 + k + 1];
+  }
+  if (k < n) s += part[s0 + k];
+  fin(x.opc, x.f0, x.f1, x.f2, s + t);
 }
 
 // Combine pass for split clades (one thread per clade).
 template <int NT, class Fin>
 __device__ __forceinline__ void run_comb(const DEntry* __restrict__ E, const DProg2& pr, const double* part,
                                          Fin fin) {
-  for (int i = threadIdx.x; i < pr.ncomb; i += NT) {
-    const ulonglong2 raw = __ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + i));
-    const Raw x = decode(raw);
-    const unsigned s0 = (unsigned)(raw.y & 0xFFFFFFFFu), n = (unsigned)(raw.y >> 32);
-    double s = part[s0];
-    for (unsigned k = 1; k < n; ++k) s += part[s0 + k];
-    fin(x.opc, x.f0, x.f1, x.f2, s);
-  }
+  for (int i = threadIdx.x; i < pr.ncomb; i += NT)
+    comb_one(__ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + i)), part, fin);
 }
 
-// The same-row levels of the root (Πroot): level after level with a barrier
-// between them.  Entries are products or the finalize op FIN (entries with
-// f0 = f1 = c): v = fma(ψ, acc, ϕ·A[c]) handed to onfin(c, v, acc); like the
-// branch rows, both take one DMUL and one DFMA so warps never diverge on FP64.
-// Levels are short, so the next level's descriptor and first entries are
-// loaded before the barrier that ends the current one.  comb(opc, c, fa, fb, s)
-// finishes split clades after an extra barrier.
-template <int NT, bool REVERSE, unsigned FIN, class OnFin, class Comb>
-__device__ __forceinline__ void run_levels(const DEntry* __restrict__ E, const DProg2* __restrict__ progs, int nlvl,
-                                           int lane, const double* A, const double* B, double* part, double ph,
-                                           double ps, OnFin onfin, Comb comb) {
-  if (nlvl <= 0) return;
-  auto at = [&](int i) { return REVERSE ? nlvl - 1 - i : i; };
-  DProg2 cur = progs[at(0)];
-  ulonglong2 pre0 = make_ulonglong2(0, (uint64_t)op::NOP << 48), pre1 = pre0;
-  if (lane < cur.nt) {
-    const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + cur.off) + lane;
-    if (cur.J > 0) pre0 = __ldg(e);
-    if (cur.J > 1) pre1 = __ldg(e + cur.nt);
-  }
-  for (int i = 0; i < nlvl; ++i) {
-    DProg2 nxt;
-    if (i + 1 < nlvl) nxt = progs[at(i + 1)];
-    if (lane < cur.nt) {
-      const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + cur.off) + lane;
-      double acc = 0.0;
-      for (int j = 0; j < cur.J; ++j) {
-        const Raw x = decode(j == 0 ? pre0 : (j == 1 ? pre1 : __ldg(e + (size_t)j * cur.nt)));
-        const bool fin = x.opc == FIN;
-        const double m = (fin ? ph : x.p) * A[x.f0];
-        const double v = fma(fin ? ps : m, fin ? acc : B[x.f1], fin ? m : acc);
-        if (x.opc == op::PROD) {
-          acc = v;
-        } else if (fin) {
-          onfin(x.f0, v, acc);
-          acc = 0.0;
-        } else if (x.opc == op::FIN_PART) {
-          part[x.f2] = acc;
-          acc = 0.0;
-        }
-      }
-    }
-    if (cur.ncomb) {
-      __syncthreads();
-      run_comb<NT>(E, cur, part, comb);
-    }
-    if (i + 1 < nlvl) {
-      pre0 = pre1 = make_ulonglong2(0, (uint64_t)op::NOP << 48);
-      if (lane < nxt.nt) {
-        const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + nxt.off) + lane;
-        if (nxt.J > 0) pre0 = __ldg(e);
-        if (nxt.J > 1) pre1 = __ldg(e + nxt.nt);
-      }
-      cur = nxt;
-    }
-    __syncthreads();
-  }
+// A thread's first combine entry of a program, held in registers while the
+// program repeats (rows of a branch) or runs later (next root level).
+struct CombReg {
+  ulonglong2 raw;
+};
+__device__ __forceinline__ CombReg load_comb(const DEntry* __restrict__ E, const DProg2& pr) {
+  CombReg c;
+  c.raw = (int)threadIdx.x < pr.ncomb ? __ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + threadIdx.x))
+                                      : make_ulonglong2(0, 0);
+  return c;
+}
+template <int NT, class Fin>
+__device__ __forceinline__ void run_comb_reg(const DEntry* __restrict__ E, const DProg2& pr, const CombReg& cr,
+                                             const double* part, Fin fin) {
+  if ((int)threadIdx.x < pr.ncomb) comb_one(cr.raw, part, fin);
+  for (int i = threadIdx.x + NT; i < pr.ncomb; i += NT)
+    comb_one(__ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + i)), part, fin);
 }
 
 // Row program of the branch recursion (PROD / FIN_DUP / FIN_PART): one DMUL and
@@ -421,29 +409,95 @@ __device__ __forceinline__ void load_lane_prog(const DEntry* __restrict__ E, con
   }
 }
 
-// One row from a register-resident program.  PROD: acc = fma(p·A[f0], B[f1],
-// acc); the finalize op FIN (entries with f0 = f1 = c): v = fma(ψ, acc,
-// ϕ·A[c]), handed to onfin(c, v, acc); FIN_PART: part[f2] = acc.
+// One entry of a lane program.  PROD: acc = fma(p·A[f0], B[f1], acc); the
+// finalize op FIN (entries with f0 = f1 = c): v = fma(ψ, acc, ϕ·A[c]),
+// handed to onfin(c, v, acc); FIN_PART: part[f2] = acc.  One DMUL and one
+// DFMA whatever the op, operands routed by selects.
+template <unsigned FIN, class OnFin>
+__device__ __forceinline__ void lane_step(unsigned f0, unsigned f1, unsigned f2, unsigned opc, double p,
+                                          const double* A, const double* B, double* part, double ph, double ps,
+                                          OnFin& onfin, double& acc) {
+  const bool fin = opc == FIN;
+  const double m = (fin ? ph : p) * A[f0];
+  const double v = fma(fin ? ps : m, fin ? acc : B[f1], fin ? m : acc);
+  if (opc == op::PROD) {
+    acc = v;
+  } else if (fin) {
+    onfin(f0, v, acc);
+    acc = 0.0;
+  } else if (opc == op::FIN_PART) {
+    part[f2] = acc;
+    acc = 0.0;
+  }
+}
+
+// The register-resident entries of a lane program (the first min(J, MAXJ)).
+template <int MAXJ, unsigned FIN, class OnFin>
+__device__ __forceinline__ void reg_steps(const LaneProg<MAXJ>& lp, const double* A, const double* B, double* part,
+                                          double ph, double ps, OnFin& onfin, double& acc) {
+#pragma unroll
+  for (int j = 0; j < MAXJ; ++j)
+    if (j < lp.J)
+      lane_step<FIN>(lp.ab[j] & 0xFFFFu, lp.ab[j] >> 16, lp.om[j] & 0xFFFFu, lp.om[j] >> 16, lp.p[j], A, B, part, ph,
+                     ps, onfin, acc);
+}
+
+// One row from a register-resident program.
 template <int MAXJ, unsigned FIN, class OnFin>
 __device__ __forceinline__ void rows_reg(const LaneProg<MAXJ>& lp, const double* A, const double* B, double* part,
                                          double ph, double ps, OnFin onfin) {
   double acc = 0.0;
-#pragma unroll
-  for (int j = 0; j < MAXJ; ++j) {
-    if (j < lp.J) {
-      const unsigned f0 = lp.ab[j] & 0xFFFFu, f1 = lp.ab[j] >> 16, opc = lp.om[j] >> 16;
-      const bool fin = opc == FIN;
-      const double m = (fin ? ph : lp.p[j]) * A[f0];
-      const double v = fma(fin ? ps : m, fin ? acc : B[f1], fin ? m : acc);
-      if (opc == op::PROD) {
-        acc = v;
-      } else if (fin) {
-        onfin(f0, v, acc);
-        acc = 0.0;
-      } else if (opc == op::FIN_PART) {
-        part[lp.om[j] & 0xFFFFu] = acc;
-        acc = 0.0;
+  reg_steps<MAXJ, FIN>(lp, A, B, part, ph, ps, onfin, acc);
+}
+
+// The same-row levels of the root (Πroot): level after level with a barrier
+// between them; entries as in lane_step (products and the finalize op FIN).
+// Levels are short and latency-bound, so each level's first kLvlJ entries
+// per lane, its first combine entry per thread and the descriptor of the
+// level after it are loaded while the level before it runs; entries past
+// kLvlJ stream from memory.  comb(opc, c, fa, fb, s) finishes split clades
+// after an extra barrier.
+constexpr int kLvlJ = 4;
+template <int NT, bool REVERSE, unsigned FIN, class OnFin, class Comb>
+__device__ __forceinline__ void run_levels(const DEntry* __restrict__ E, const DProg2* __restrict__ progs, int nlvl,
+                                           int lane, const double* A, const double* B, double* part, double ph,
+                                           double ps, OnFin onfin, Comb comb) {
+  if (nlvl <= 0) return;
+  auto at = [&](int i) { return REVERSE ? nlvl - 1 - i : i; };
+  DProg2 cur = progs[at(0)];
+  DProg2 nxt = nlvl > 1 ? progs[at(1)] : cur;
+  LaneProg<kLvlJ> lp;
+  load_lane_prog<kLvlJ>(E, cur, lane, lp);
+  CombReg cr = load_comb(E, cur);
+  for (int i = 0; i < nlvl; ++i) {
+    const bool more = i + 1 < nlvl;
+    LaneProg<kLvlJ> lpn;
+    CombReg crn = cr;
+    DProg2 nn = nxt;
+    if (more) {
+      load_lane_prog<kLvlJ>(E, nxt, lane, lpn);
+      crn = load_comb(E, nxt);
+      if (i + 2 < nlvl) nn = progs[at(i + 2)];
+    }
+    if (lane < cur.nt) {
+      double acc = 0.0;
+      reg_steps<kLvlJ, FIN>(lp, A, B, part, ph, ps, onfin, acc);
+      const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + cur.off) + lane;
+      for (int j = kLvlJ; j < cur.J; ++j) {
+        const Raw x = decode(__ldg(e + (size_t)j * cur.nt));
+        lane_step<FIN>(x.f0, x.f1, x.f2, x.opc, x.p, A, B, part, ph, ps, onfin, acc);
       }
+    }
+    if (cur.ncomb) {
+      __syncthreads();
+      run_comb_reg<NT>(E, cur, cr, part, comb);
+    }
+    __syncthreads();
+    if (more) {
+      cur = nxt;
+      nxt = nn;
+      lp = lpn;
+      cr = crn;
     }
   }
 }
@@ -461,6 +515,7 @@ __device__ __forceinline__ void fwd_rows(const DEntry* __restrict__ E, const DTa
   const DProg2 dup = T.dup;  // held in registers: the rows store to global memory
   LaneProg<J> lp;
   load_lane_prog<J>(E, dup, lane, lp);
+  const CombReg cr = load_comb(E, dup);
   const bool active = lane < dup.nt;
   for (int r = 1; r < n; ++r) {
     const double ph = phs[r], ps = pss[r];
@@ -474,7 +529,7 @@ __device__ __forceinline__ void fwd_rows(const DEntry* __restrict__ E, const DTa
     if (dup.ncomb) {
       __syncthreads();
       const double* cc = cur;
-      run_comb<NT>(E, dup, part, [&](unsigned, unsigned c, unsigned, unsigned, double s) {
+      run_comb_reg<NT>(E, dup, cr, part, [&](unsigned, unsigned c, unsigned, unsigned, double s) {
         const double v = fma(ps, s, ph * cc[c]);
         o[c] = v;
         if (TABLES) tr[c] = v;
@@ -492,6 +547,7 @@ __device__ __forceinline__ void fwd_rows_generic(const DEntry* __restrict__ E, c
                                                  const double* phs, const double* pss, double*& cur, double*& nxt,
                                                  double* part, double* tab0) {
   const DProg2 dup = T.dup;
+  const CombReg cr = load_comb(E, dup);
   for (int r = 1; r < n; ++r) {
     const double ph = phs[r], ps = pss[r];
     double* tr = TABLES ? tab0 + (int64_t)r * R : nullptr;
@@ -500,7 +556,7 @@ __device__ __forceinline__ void fwd_rows_generic(const DEntry* __restrict__ E, c
       __syncthreads();
       const double* cc = cur;
       double* o = nxt;
-      run_comb<NT>(E, dup, part, [&](unsigned, unsigned c, unsigned, unsigned, double s) {
+      run_comb_reg<NT>(E, dup, cr, part, [&](unsigned, unsigned c, unsigned, unsigned, double s) {
         const double v = fma(ps, s, ph * cc[c]);
         o[c] = v;
         if (TABLES) tr[c] = v;
@@ -529,7 +585,10 @@ __device__ __forceinline__ bool fwd_rows_dispatch(int j, const DEntry* __restric
   }
 }
 
-template <bool TABLES, int NT>
+// ROOT: the launch of the top level, whose tasks are all root tasks; the other
+// launches hold no root task.  Separate instantiations keep the root-row
+// machinery out of the register budget of the branch kernels.
+template <bool TABLES, int NT, bool ROOT = false>
 __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restrict__ list) {
   extern __shared__ double sm[];
   const DTask& T = A.tasks[list[blockIdx.x]];
@@ -545,7 +604,17 @@ __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restri
   const int roff = A.row_off[k];
   const int NR = A.NR;
   const DEntry* E = A.entries;
-  if (mn.x == WG_NODE_LEAF) {
+  if (!ROOT) {
+    prefetch_prog(E, T.dup, lane);
+    prefetch_prog(E, T.init, lane);
+    for (int r = tid; r < mn.w; r += NT) {
+      prefetch_l1(A.params + NR + roff + r);
+      prefetch_l1(A.params + 2 * NR + roff + r);
+    }
+  } else {
+    prefetch_prog(E, T.init, lane);
+  }
+  if (!ROOT && mn.x == WG_NODE_LEAF) {
     const int* aux = A.meta + T.aux;
     const double lp = A.leafp[k];
     for (int c = tid; c < R; c += NT) cur[c] = aux[c] ? lp : 0.0;
@@ -555,7 +624,7 @@ __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restri
     __syncthreads();
     const double* X = nxt;
     const double* Y = nxt + T.wa;
-    if (mn.x == WG_NODE_WGD) {
+    if (!ROOT && mn.x == WG_NODE_WGD) {
       const double q = A.params[3 * NR + k];
       const double ef = eps_top2(A, mn.y);
       auto fin = [&](unsigned, unsigned c, unsigned fa, unsigned, double acc) {
@@ -579,15 +648,11 @@ __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restri
         __syncthreads();
         run_comb<NT>(E, T.init, part, fin);
       }
-      if (mn.x == WG_NODE_ROOT) {
+      if (ROOT) {
         // whaleroot! (src/core.jl:130-149), Πroot over smaller clades of the
         // same row: level by level, in place
         __syncthreads();
-        const double eta = A.params[3 * NR + A.K];
-        const double er = eps_top2(A, k);
-        const double xi = 1.0 - (1.0 - eta) * er;
-        const double ca = (1.0 - eta) * xi / eta;
-        const double cb = eta * (1.0 - er) / (xi * xi);
+        const double ca = A.params[3 * NR + A.K + 1], cb = A.params[3 * NR + A.K + 2];
         auto lcomb = [&](unsigned, unsigned c, unsigned, unsigned, double acc) { cur[c] = fma(ca, acc, cb * cur[c]); };
         run_levels<NT, false, op::FIN_LVL>(E, A.progs + T.lvl, T.nlvl, lane, cur, cur, part, cb, ca,
                                            [&](unsigned c, double v, double) { cur[c] = v; }, lcomb);
@@ -597,7 +662,7 @@ __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restri
   __syncthreads();
   if (TABLES)
     for (int c = tid; c < R; c += NT) A.tabs[T.tab + c] = cur[c];
-  if (mn.x != WG_NODE_ROOT && mn.w > 1) {
+  if (!ROOT && mn.w > 1) {
     double* phs = part + T.nslot_max;  // ϕ, ψ of this branch's rows
     double* pss = phs + mn.w;
     for (int r = tid; r < mn.w; r += NT) {
@@ -611,7 +676,7 @@ __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restri
   }
   double* top = A.tops + T.top;
   for (int c = tid; c < R; c += NT) top[c] = cur[c];
-  if (mn.x == WG_NODE_ROOT) {
+  if (ROOT) {
     const int2* fam = reinterpret_cast<const int2*>(A.meta) + T.fam;
     for (int f = tid; f < T.nfam; f += NT) {
       const int2 fp = fam[f];
@@ -751,6 +816,7 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
     }
     if (td.ncomb) {
       __syncthreads();
+      // (combine entries stream from memory here: registers are the limit)
       run_comb<NT>(E, td, part, [&](unsigned, unsigned c, unsigned, unsigned, double g) {
         bn[c] = fma(ps, g, ph * bb[c]);
         Gs[c] = g;
@@ -808,7 +874,8 @@ __device__ __forceinline__ bool adj_rows_dispatch(int j, const DEntry* __restric
   }
 }
 
-template <int NT>
+// ROOT as for k_fwd2.
+template <int NT, bool ROOT = false>
 __global__ void __launch_bounds__(NT, NT == 128 ? 6 : 2) k_adj2(const KArgs2 A, const int* __restrict__ list) {
   extern __shared__ double sm[];
   const DTask& T = A.tasks[list[blockIdx.x]];
@@ -827,13 +894,24 @@ __global__ void __launch_bounds__(NT, NT == 128 ? 6 : 2) k_adj2(const KArgs2 A, 
   double* L1 = sm + 3 * W2;
   double* Gs = sm + 5 * W2;
   double* part = sm + 6 * W2;
-  int ms = max(max(T.tdup.nslot, T.ta.nslot), max(T.tb.nslot, T.init.nslot));
-  for (int q = 0; q < T.nlvl; ++q) ms = max(ms, A.progs[T.tlvl + q].nslot);
-  double* red = part + ms;  // 16 * warps doubles
+  double* red = part + T.nslot_max;  // 16 * warps doubles
   double* out = A.gout + T.gout;
   const DEntry* E = A.entries;
   const int64_t* gm = A.gmap + T.gmap;
-  if (mn.x == WG_NODE_ROOT) {
+  if (!ROOT) {
+    prefetch_prog(E, T.tdup, lane);
+    prefetch_prog(E, T.ta, lane);
+    prefetch_prog(E, T.tb, lane);
+    for (int r = tid; r < n; r += NT) {
+      prefetch_l1(A.params + NR + roff + r);
+      prefetch_l1(A.params + 2 * NR + roff + r);
+    }
+  } else {
+    prefetch_prog(E, T.init, lane);
+    prefetch_prog(E, T.ta, lane);
+    prefetch_prog(E, T.tb, lane);
+  }
+  if (ROOT) {
     const double* row0 = A.tabs + T.tab;
     for (int c = tid; c < R; c += NT) {
       L0[c] = row0[c];
@@ -846,11 +924,7 @@ __global__ void __launch_bounds__(NT, NT == 128 ? 6 : 2) k_adj2(const KArgs2 A, 
       bar[fam[f].y] = L > 0.0 ? 1.0 / L : 0.0;
     }
     __syncthreads();
-    const double eta = A.params[3 * NR + A.K];
-    const double er = eps_top2(A, k);
-    const double xi = 1.0 - (1.0 - eta) * er;
-    const double ca = (1.0 - eta) * xi / eta;
-    const double cb = eta * (1.0 - er) / (xi * xi);
+    const double ca = A.params[3 * NR + A.K + 1], cb = A.params[3 * NR + A.K + 2];
     double acc4[4] = {0.0, 0.0, 0.0, 0.0};  // dca, dcb, dea, deb
     for (int c = tid; c < R; c += NT) Gs[c] = 0.0;
     __syncthreads();
@@ -912,6 +986,9 @@ __global__ void __launch_bounds__(NT, NT == 128 ? 6 : 2) k_adj2(const KArgs2 A, 
     }
     block_sum4<NT>(acc4, red);
     if (tid == 0) {
+      const double eta = A.params[3 * NR + A.K];
+      const double er = eps_top2(A, k);
+      const double xi = 1.0 - (1.0 - eta) * er;
       const double dxi_deta = er, dxi_der = -(1.0 - eta);
       const double dca_deta = (-xi + (1.0 - eta) * dxi_deta) / eta - (1.0 - eta) * xi / (eta * eta);
       const double dca_der = (1.0 - eta) * dxi_der / eta;
@@ -1336,6 +1413,12 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
       b->fam_sub[ids[i]] = (int)b->subs.size();
       b->fam_local[ids[i]] = (int)i;
     }
+    if (!P.levels_h.empty() && !P.levels_h.back().empty())
+      throw Error(WG_ESTATE, "internal: heavy task at the root level");
+    for (size_t L = 0; L < P.levels.size(); ++L)
+      for (int t : P.levels[L])
+        if ((m->kind[P.tasks[t].node] == WG_NODE_ROOT) != (L + 1 == P.levels.size()))
+          throw Error(WG_ESTATE, "internal: root tasks must form the top level");
     std::vector<int> lists;
     for (size_t L = 0; L < P.levels.size(); ++L) {
       sb->lvl_off.push_back((int)lists.size());
@@ -1384,10 +1467,10 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
       ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
     b->subs.push_back(std::move(sb));
   }
-  b->d_params = dalloc<double>(b->P, by);
+  b->d_params = dalloc<double>(b->P + 2, by);
   b->d_logl = dalloc<double>(n, by);
   upload_model_static(b.get(), m, s);
-  ck(cudaMallocHost(&b->h_params, sizeof(double) * b->P), "cudaMallocHost");
+  ck(cudaMallocHost(&b->h_params, sizeof(double) * (b->P + 2)), "cudaMallocHost");
   ck(cudaMallocHost(&b->h_logl, sizeof(double) * n), "cudaMallocHost");
   if (adjoint) ck(cudaMallocHost(&b->h_gred, sizeof(double) * b->P * b->subs.size()), "cudaMallocHost");
   ck(cudaStreamSynchronize(s), "batch upload");
@@ -1455,6 +1538,28 @@ void join_subs(wg_batch* b) {
   }
 }
 
+// Parameters of one evaluation in the pinned staging buffer: ε, ϕ, ψ per row,
+// q per node, η, then the root-row constants of whaleroot! (src/core.jl:
+// 130-149) ca = (1-η)ξ/η and cb = η(1-ε)/ξ² with ξ = 1-(1-η)ε, ε the top ε of
+// the root, which every root task would otherwise recompute.
+void stage_params(wg_batch* b, const wg_model* m) {
+  const int NR = b->NR, K = b->K;
+  double* h = b->h_params;
+  std::memcpy(h, m->eps.data(), NR * sizeof(double));
+  std::memcpy(h + NR, m->phi.data(), NR * sizeof(double));
+  std::memcpy(h + 2 * NR, m->psi.data(), NR * sizeof(double));
+  for (int k = 0; k < K; ++k) h[3 * NR + k] = std::isnan(m->q[k]) ? 0.0 : m->q[k];
+  const double eta = m->eta;
+  h[3 * NR + K] = eta;
+  int root = -1;
+  for (int k = 0; k < K; ++k)
+    if (m->kind[k] == WG_NODE_ROOT) root = k;
+  const double er = root >= 0 ? m->eps_top(root) : 0.0;
+  const double xi = 1.0 - (1.0 - eta) * er;
+  h[3 * NR + K + 1] = (1.0 - eta) * xi / eta;
+  h[3 * NR + K + 2] = eta * (1.0 - er) / (xi * xi);
+}
+
 // Every class's forward levels (and the reverse levels of the adjoint plus
 // its gradient reduction), forked from and joined back to the context stream.
 void record_sequence(wg_batch* b, bool grad, bool tables) {
@@ -1462,7 +1567,8 @@ void record_sequence(wg_batch* b, bool grad, bool tables) {
   cudaStream_t s = ctx->stream;
   int& nl = b->launches[grad ? 1 : 0];
   nl = 0;
-  ck(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(double) * b->P, cudaMemcpyHostToDevice, s), "params upload");
+  ck(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(double) * (b->P + 2), cudaMemcpyHostToDevice, s),
+     "params upload");
   if (grad)
     for (auto& sb : b->subs)
       ck(cudaMemsetAsync(sb->d_gout, 0, sizeof(double) * (size_t)sb->gout_doubles, s), "memset");
@@ -1471,6 +1577,7 @@ void record_sequence(wg_batch* b, bool grad, bool tables) {
   for (auto& sbp : b->subs) {
     SubBatch* sb = sbp.get();
     const KArgs2 A = sub_args(b, sb);
+    const int top = (int)sb->lvl_n.size() - 1;  // the root level
     for (int L = 0; L < (int)sb->lvl_n.size(); ++L) {
       const int* ll = sb->d_lists + sb->lvl_off[L];
       const int* lh = sb->d_lists + sb->lvlh_off[L];
@@ -1478,8 +1585,12 @@ void record_sequence(wg_batch* b, bool grad, bool tables) {
           sb, L,
           [&](cudaStream_t st) {
             ++nl;
-            if (tables) k_fwd2<true, kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem[L], st>>>(A, ll);
-            else k_fwd2<false, kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem[L], st>>>(A, ll);
+            const dim3 g(sb->lvl_n[L]);
+            const size_t sm = sb->lvl_smem[L];
+            if (L == top && tables) k_fwd2<true, kNT2L, true><<<g, kNT2L, sm, st>>>(A, ll);
+            else if (L == top) k_fwd2<false, kNT2L, true><<<g, kNT2L, sm, st>>>(A, ll);
+            else if (tables) k_fwd2<true, kNT2L><<<g, kNT2L, sm, st>>>(A, ll);
+            else k_fwd2<false, kNT2L><<<g, kNT2L, sm, st>>>(A, ll);
           },
           [&](cudaStream_t st) {
             ++nl;
@@ -1496,6 +1607,7 @@ void record_sequence(wg_batch* b, bool grad, bool tables) {
     for (auto& sbp : b->subs) {
       SubBatch* sb = sbp.get();
       const KArgs2 A = sub_args(b, sb);
+      const int top = (int)sb->lvl_n.size() - 1;
       for (int L = (int)sb->lvl_n.size() - 1; L >= 0; --L) {
         const int* ll = sb->d_lists + sb->lvl_off[L];
         const int* lh = sb->d_lists + sb->lvlh_off[L];
@@ -1503,7 +1615,8 @@ void record_sequence(wg_batch* b, bool grad, bool tables) {
             sb, L,
             [&](cudaStream_t st) {
               ++nl;
-              k_adj2<kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem_adj[L], st>>>(A, ll);
+              if (L == top) k_adj2<kNT2L, true><<<sb->lvl_n[L], kNT2L, sb->lvl_smem_adj[L], st>>>(A, ll);
+              else k_adj2<kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem_adj[L], st>>>(A, ll);
             },
             [&](cudaStream_t st) {
               ++nl;
@@ -1532,12 +1645,7 @@ void enqueue(wg_batch* b, const wg_model* m, bool grad) {
     if (!e) ck(cudaEventCreate(&e), "cudaEventCreate");
   // the pinned parameter buffer is read by the previous launch's copy
   if (b->pending) ck(cudaStreamSynchronize(ctx->stream), "pending evaluation");
-  const int NR = b->NR, K = b->K;
-  std::memcpy(b->h_params, m->eps.data(), NR * sizeof(double));
-  std::memcpy(b->h_params + NR, m->phi.data(), NR * sizeof(double));
-  std::memcpy(b->h_params + 2 * NR, m->psi.data(), NR * sizeof(double));
-  for (int k = 0; k < K; ++k) b->h_params[3 * NR + k] = std::isnan(m->q[k]) ? 0.0 : m->q[k];
-  b->h_params[3 * NR + K] = m->eta;
+  stage_params(b, m);
   const bool tables = grad || (b->flags & WG_BATCH_TABLES);
   cudaGraphExec_t& ge = b->graph[grad][tables];
   cudaStream_t s = ctx->stream;
@@ -1666,6 +1774,9 @@ int wg_ctx_create(int device, wg_ctx** out) {
     ck(cudaFuncSetAttribute(k_fwd2<false, kNT2H>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
     ck(cudaFuncSetAttribute(k_fwd2<true, kNT2H>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
     ck(cudaFuncSetAttribute(k_adj2<kNT2L>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    ck(cudaFuncSetAttribute(k_fwd2<false, kNT2L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    ck(cudaFuncSetAttribute(k_fwd2<true, kNT2L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    ck(cudaFuncSetAttribute(k_adj2<kNT2L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
     ck(cudaFuncSetAttribute(k_adj2<kNT2H>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
     *out = c.release();
   });
@@ -1903,13 +2014,9 @@ extern "C" int wg_logpdf_noalloc(wg_ctx* ctx, wg_model* m, wg_batch* b, double* 
     double* scratch = noalloc_scratch(ctx->device);
     cudaStream_t s = ctx->stream;
     if (b->pending) ck(cudaStreamSynchronize(s), "pending evaluation");
-    const int NR = b->NR, K = b->K;
-    std::memcpy(b->h_params, m->eps.data(), NR * sizeof(double));
-    std::memcpy(b->h_params + NR, m->phi.data(), NR * sizeof(double));
-    std::memcpy(b->h_params + 2 * NR, m->psi.data(), NR * sizeof(double));
-    for (int k = 0; k < K; ++k) b->h_params[3 * NR + k] = std::isnan(m->q[k]) ? 0.0 : m->q[k];
-    b->h_params[3 * NR + K] = m->eta;
-    ck(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(double) * b->P, cudaMemcpyHostToDevice, s), "params upload");
+    stage_params(b, m);
+    ck(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(double) * (b->P + 2), cudaMemcpyHostToDevice, s),
+       "params upload");
     // every top row is written by its task before a parent reads it, so the
     // scratch needs no clearing; it keeps the last call's rows afterwards
     int64_t off = 0;
@@ -1922,7 +2029,9 @@ extern "C" int wg_logpdf_noalloc(wg_ctx* ctx, wg_model* m, wg_batch* b, double* 
       for (int L = 0; L < (int)sb->lvl_n.size(); ++L) {
         if (sb->lvlh_n[L] > 0)
           k_fwd2<false, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], s>>>(A, sb->d_lists + sb->lvlh_off[L]);
-        if (sb->lvl_n[L] > 0)
+        if (sb->lvl_n[L] > 0 && L + 1 == (int)sb->lvl_n.size())
+          k_fwd2<false, kNT2L, true><<<sb->lvl_n[L], kNT2L, sb->lvl_smem[L], s>>>(A, sb->d_lists + sb->lvl_off[L]);
+        else if (sb->lvl_n[L] > 0)
           k_fwd2<false, kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem[L], s>>>(A, sb->d_lists + sb->lvl_off[L]);
       }
     }

@@ -930,7 +930,8 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       }
       // shared memory: cur + nxt rows (children staged in nxt) + slots + spare
       int slots = std::max({T.dup.nslot, T.init.nslot, T.tdup.nslot, T.ta.nslot, T.tb.nslot});
-      for (int64_t q = T.lvl; q < (int64_t)P.progs.size(); ++q) slots = std::max(slots, P.progs[q].nslot);
+      if (T.nlvl > 0)  // the root's level programs (forward and transposed) are the last ones pushed
+        for (int64_t q = T.lvl; q < (int64_t)P.progs.size(); ++q) slots = std::max(slots, P.progs[q].nslot);
       // forward: cur, nxt (children staged in nxt); adjoint: bar, barn, two
       // L rows, G; then partial slots and reduction scratch
       const int W2 = std::max(R, T.wa + T.wb);
