@@ -220,9 +220,9 @@ struct DTask {
   DProg2 tdup;          // adjoint of rows >= 1 (and WGD row 0)
   DProg2 ta, tb;        // adjoint of the speciation row 0, per child
   int32_t nlvl = 0;     // root: levels of the same-row recursion
-  int32_t _pad = 0;
-  int64_t lvl = 0;      // first DProg2 of the level programs (forward)
-  int64_t tlvl = 0;     // first DProg2 of the level programs (adjoint)
+  int32_t rslot = 0;    // root: partial slots of the level programs
+  int64_t lvl = 0;      // root: first DProg2 of the level programs (forward)
+  int64_t tlvl = 0;     // root: first DProg2 of the level programs (adjoint)
   int64_t fam = 0;      // root: int2 per family (family index, ubiquitous position)
   int64_t gout = 0;     // adjoint: per-task outputs, 2 * nrow + 5 doubles
 };
@@ -255,6 +255,11 @@ struct PackOptions2 {
   int64_t target_ops = 480;   // forward product + finalize ops per row per task
   int64_t heavy_ops = 1024;   // non-root tasks above this many ops per row get kNT2H threads
   int64_t max_width = 6144;   // cap on a task's row width
+  // Root tasks run their same-row levels one after another, each short and
+  // latency-bound, so they take target_ops * root_group ops (all levels
+  // together), up to max_width_root clades (their adjoint keeps six rows).
+  int root_group = 16;
+  int64_t max_width_root = 1536;
   int target_j = 3;           // iterations per row the lane scheduler aims for
   bool keep_tables = false;
   bool adjoint = false;

@@ -335,17 +335,18 @@ __device__ __forceinline__ void run_comb(const DEntry* __restrict__ E, const DPr
 struct CombReg {
   ulonglong2 raw;
 };
-__device__ __forceinline__ CombReg load_comb(const DEntry* __restrict__ E, const DProg2& pr) {
+// tix: the thread's index among the NT threads that share the program.
+__device__ __forceinline__ CombReg load_comb(const DEntry* __restrict__ E, const DProg2& pr,
+                                             int tix = (int)threadIdx.x) {
   CombReg c;
-  c.raw = (int)threadIdx.x < pr.ncomb ? __ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + threadIdx.x))
-                                      : make_ulonglong2(0, 0);
+  c.raw = tix < pr.ncomb ? __ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + tix)) : make_ulonglong2(0, 0);
   return c;
 }
 template <int NT, class Fin>
 __device__ __forceinline__ void run_comb_reg(const DEntry* __restrict__ E, const DProg2& pr, const CombReg& cr,
-                                             const double* part, Fin fin) {
-  if ((int)threadIdx.x < pr.ncomb) comb_one(cr.raw, part, fin);
-  for (int i = threadIdx.x + NT; i < pr.ncomb; i += NT)
+                                             const double* part, Fin fin, int tix = (int)threadIdx.x) {
+  if (tix < pr.ncomb) comb_one(cr.raw, part, fin);
+  for (int i = tix + NT; i < pr.ncomb; i += NT)
     comb_one(__ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + i)), part, fin);
 }
 
@@ -450,49 +451,55 @@ __device__ __forceinline__ void rows_reg(const LaneProg<MAXJ>& lp, const double*
   reg_steps<MAXJ, FIN>(lp, A, B, part, ph, ps, onfin, acc);
 }
 
-// The same-row levels of the root (Πroot): level after level with a barrier
-// between them; entries as in lane_step (products and the finalize op FIN).
-// Levels are short and latency-bound, so each level's first kLvlJ entries
-// per lane, its first combine entry per thread and the descriptor of the
-// level after it are loaded while the level before it runs; entries past
-// kLvlJ stream from memory.  comb(opc, c, fa, fb, s) finishes split clades
-// after an extra barrier.
+// The same-row levels of a root row (Πroot), run by the NTG threads of the
+// CTA for all the task's families in lock step: level after level with a
+// barrier between them; entries as in lane_step (products and the
+// finalize op FIN).  Levels are short and latency-bound, so each level's
+// first kLvlJ entries per lane, its first combine entry per thread and the
+// descriptor of the level after it are loaded while the level before it
+// runs; entries past kLvlJ stream from memory.  comb(opc, c, fa, fb, s)
+// finishes split clades after a barrier.  wl: lane in the program, tix:
+// thread index among the NTG.
 constexpr int kLvlJ = 4;
-template <int NT, bool REVERSE, unsigned FIN, class OnFin, class Comb>
-__device__ __forceinline__ void run_levels(const DEntry* __restrict__ E, const DProg2* __restrict__ progs, int nlvl,
-                                           int lane, const double* A, const double* B, double* part, double ph,
-                                           double ps, OnFin onfin, Comb comb) {
+template <int NTG, bool REVERSE, unsigned FIN, class OnFin, class Comb>
+__device__ __forceinline__ void chain_levels(const DEntry* __restrict__ E, const DProg2* __restrict__ progs, int nlvl,
+                                             int wl, int tix, const double* A, const double* B, double* part,
+                                             double ph, double ps, OnFin onfin, Comb comb) {
+  auto sync = [] {
+    if (NTG == 32) __syncwarp();
+    else __syncthreads();
+  };
   if (nlvl <= 0) return;
   auto at = [&](int i) { return REVERSE ? nlvl - 1 - i : i; };
   DProg2 cur = progs[at(0)];
   DProg2 nxt = nlvl > 1 ? progs[at(1)] : cur;
   LaneProg<kLvlJ> lp;
-  load_lane_prog<kLvlJ>(E, cur, lane, lp);
-  CombReg cr = load_comb(E, cur);
+  load_lane_prog<kLvlJ>(E, cur, wl, lp);
+  CombReg cr = load_comb(E, cur, tix);
   for (int i = 0; i < nlvl; ++i) {
     const bool more = i + 1 < nlvl;
     LaneProg<kLvlJ> lpn;
     CombReg crn = cr;
     DProg2 nn = nxt;
     if (more) {
-      load_lane_prog<kLvlJ>(E, nxt, lane, lpn);
-      crn = load_comb(E, nxt);
+      load_lane_prog<kLvlJ>(E, nxt, wl, lpn);
+      crn = load_comb(E, nxt, tix);
       if (i + 2 < nlvl) nn = progs[at(i + 2)];
     }
-    if (lane < cur.nt) {
+    if (wl < cur.nt) {
       double acc = 0.0;
       reg_steps<kLvlJ, FIN>(lp, A, B, part, ph, ps, onfin, acc);
-      const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + cur.off) + lane;
+      const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + cur.off) + wl;
       for (int j = kLvlJ; j < cur.J; ++j) {
         const Raw x = decode(__ldg(e + (size_t)j * cur.nt));
         lane_step<FIN>(x.f0, x.f1, x.f2, x.opc, x.p, A, B, part, ph, ps, onfin, acc);
       }
     }
     if (cur.ncomb) {
-      __syncthreads();
-      run_comb_reg<NT>(E, cur, cr, part, comb);
+      sync();
+      run_comb_reg<NTG>(E, cur, cr, part, comb, tix);
     }
-    __syncthreads();
+    sync();
     if (more) {
       cur = nxt;
       nxt = nn;
@@ -654,8 +661,9 @@ __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restri
         __syncthreads();
         const double ca = A.params[3 * NR + A.K + 1], cb = A.params[3 * NR + A.K + 2];
         auto lcomb = [&](unsigned, unsigned c, unsigned, unsigned, double acc) { cur[c] = fma(ca, acc, cb * cur[c]); };
-        run_levels<NT, false, op::FIN_LVL>(E, A.progs + T.lvl, T.nlvl, lane, cur, cur, part, cb, ca,
-                                           [&](unsigned c, double v, double) { cur[c] = v; }, lcomb);
+        auto lfin = [&](unsigned c, double v, double) { cur[c] = v; };
+        chain_levels<NT, false, op::FIN_LVL>(E, A.progs + T.lvl, T.nlvl, lane, tid, cur, cur, part, cb, ca, lfin,
+                                             lcomb);
       }
     }
   }
@@ -932,12 +940,12 @@ __global__ void __launch_bounds__(NT, NT == 128 ? 6 : 2) k_adj2(const KArgs2 A, 
       bar[c] = fma(ca, g, bar[c]);
       Gs[c] = g;
     };
-    run_levels<NT, true, op::FIN_TLVL>(E, A.progs + T.tlvl, T.nlvl, lane, bar, L0, part, 1.0, ca,
-                                       [&](unsigned c, double v, double g) {
-                                         bar[c] = v;
-                                         Gs[c] = g;
-                                       },
-                                       tcomb);
+    auto tfin = [&](unsigned c, double v, double g) {
+      bar[c] = v;
+      Gs[c] = g;
+    };
+    chain_levels<NT, true, op::FIN_TLVL>(E, A.progs + T.tlvl, T.nlvl, lane, tid, bar, L0, part, 1.0, ca, tfin,
+                                         tcomb);
     // ∂/∂ca = Σ bar[γ]·Πroot(γ) = ½ Σ_x G[x]·L[x] (each split counted twice)
     for (int c = tid; c < R; c += NT) acc4[0] += 0.5 * Gs[c] * L0[c];
     // stage the children's tops, recompute Πspec + Πloss for ∂/∂cb

@@ -695,12 +695,17 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
     std::vector<std::vector<int>> groups;
     std::vector<double> group_ops;
     {
+      // the root row is a chain of short same-row levels, so a root task
+      // takes many more families for the same per-level work
+      const bool is_root = kind == WG_NODE_ROOT;
+      const double tops_lim = is_root ? (double)opt.target_ops * opt.root_group : (double)opt.target_ops;
+      const int64_t wlim = is_root ? opt.max_width_root : opt.max_width;
       std::vector<int> cur;
       double ops = 0;
       int64_t width = 0;
       for (auto& [w, f] : fw) {
         const int C = info[f].ncompat[k];
-        if (!cur.empty() && (ops + w > opt.target_ops || width + C > opt.max_width)) {
+        if (!cur.empty() && (ops + w > tops_lim || width + C > wlim)) {
           groups.push_back(cur);
           group_ops.push_back(ops);
           cur.clear();
@@ -881,11 +886,12 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
         }
       }
       if (kind == WG_NODE_ROOT) {
+        // Πroot (same-row recursion over split levels): the levels of all the
+        // task's families in lock step, one program per level for the CTA
         int nl = 0;
         for (int i = 0; i < nf; ++i)
           for (int v : lvl[fams[i]]) nl = std::max(nl, v + 1);
         std::vector<std::vector<Item>> lw(nl), tlw(nl);
-        std::vector<std::vector<int>> lvl_of_pos;
         std::vector<int> plevel(R, 0);
         for (int i = 0; i < nf; ++i) {
           const CCD& c = *ccds[fams[i]];
@@ -923,6 +929,10 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
           T.tlvl = (int64_t)P.progs.size();
           for (int L = 0; L < nl; ++L) P.progs.push_back(schedule2(tlw[L], NT, opt.target_j, P.entries));
         }
+        for (int64_t q = T.lvl; q < (int64_t)P.progs.size(); ++q) T.rslot = std::max(T.rslot, P.progs[q].nslot);
+      }
+      if (kind == WG_NODE_ROOT) {
+        // log L outputs: family index and position of its ubiquitous clade
         std::vector<std::array<int, 2>> fam(nf);
         for (int i = 0; i < nf; ++i)
           fam[i] = {opt.global_ids ? (*opt.global_ids)[fams[i]] : fams[i], pos(i, ccds[fams[i]]->n_clades - 1)};
@@ -930,8 +940,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       }
       // shared memory: cur + nxt rows (children staged in nxt) + slots + spare
       int slots = std::max({T.dup.nslot, T.init.nslot, T.tdup.nslot, T.ta.nslot, T.tb.nslot});
-      if (T.nlvl > 0)  // the root's level programs (forward and transposed) are the last ones pushed
-        for (int64_t q = T.lvl; q < (int64_t)P.progs.size(); ++q) slots = std::max(slots, P.progs[q].nslot);
+      slots = std::max(slots, T.rslot);  // root: the level programs' partial slots
       // forward: cur, nxt (children staged in nxt); adjoint: bar, barn, two
       // L rows, G; then partial slots and reduction scratch
       const int W2 = std::max(R, T.wa + T.wb);
