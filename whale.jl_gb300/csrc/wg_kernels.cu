@@ -882,9 +882,11 @@ __device__ __forceinline__ bool adj_rows_dispatch(int j, const DEntry* __restric
   }
 }
 
-// ROOT as for k_fwd2.
+// ROOT as for k_fwd2.  Four 128-thread CTAs per SM leave the adjoint its
+// ~120 registers: at five or six the spills cost more than the occupancy
+// gains (the rows are latency-bound, not FP64-bound).
 template <int NT, bool ROOT = false>
-__global__ void __launch_bounds__(NT, NT == 128 ? 6 : 2) k_adj2(const KArgs2 A, const int* __restrict__ list) {
+__global__ void __launch_bounds__(NT, NT == 128 ? 4 : 2) k_adj2(const KArgs2 A, const int* __restrict__ list) {
   extern __shared__ double sm[];
   const DTask& T = A.tasks[list[blockIdx.x]];
   const int k = T.node;
