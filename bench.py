@@ -103,7 +103,7 @@ class ClockSampler:
 # DRAM bytes per evaluation of the 5,000-family workload, summed over the
 # launches of each kernel family, from the ncu launch list kept in
 # profiles/launches_cfg1_5000fam.txt (not measurable inside the timed run).
-NCU_DRAM_BYTES = {"adjoint": 777_427_712, "forward": 370_898_432}
+NCU_DRAM_BYTES = {"adjoint": 748_317_184, "forward": 349_949_440}
 
 
 def workload(nf):
