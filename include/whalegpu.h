@@ -55,6 +55,9 @@ extern "C" {
 /* wg_batch_create flags */
 #define WG_BATCH_GRAD 1u   /* keep device space for the adjoint's DP tables */
 #define WG_BATCH_TABLES 2u /* keep device space to return every DP table (logpdf!) */
+/* Every task keeps its working rows in device memory, as the tasks too wide
+ * for shared memory always do (a testing aid for that path; slower). */
+#define WG_BATCH_SCRATCH_ROWS 4u
 
 typedef struct wg_ctx wg_ctx;
 typedef struct wg_model wg_model;

@@ -64,11 +64,14 @@ class Batch:
     """Device-resident packed families (wg_batch) for one model structure."""
 
     def __init__(self, wm: WhaleModel, ccds: Sequence[CCD], grad: bool = False, tables: bool = False,
-                 ctx: Context = None):
+                 ctx: Context = None, scratch_rows: bool = False):
+        """scratch_rows: every task keeps its working rows in device memory,
+        as tasks too wide for shared memory always do (testing aid)."""
         self.ctx = ctx or default_context()
         self.ccds = list(ccds)
         self.n = len(self.ccds)
-        flags = (N.BATCH_GRAD if grad else 0) | (N.BATCH_TABLES if tables else 0)
+        flags = ((N.BATCH_GRAD if grad else 0) | (N.BATCH_TABLES if tables else 0)
+                 | (N.BATCH_SCRATCH_ROWS if scratch_rows else 0))
         arr = (N.C.c_void_p * self.n)(*[c._h for c in self.ccds])
         h = N.vp()
         N.check(N.lib().wg_batch_create(self.ctx.h, wm._struct.h, arr, self.n, flags, N.C.byref(h)))

@@ -225,6 +225,10 @@ struct DTask {
   int64_t tlvl = 0;     // root: first DProg2 of the level programs (adjoint)
   int64_t fam = 0;      // root: int2 per family (family index, ubiquitous position)
   int64_t gout = 0;     // adjoint: per-task outputs, 2 * nrow + 5 doubles
+  int64_t scratch = -1;  // rows wider than shared memory: offset of the task's working rows in the
+                         // batch's device scratch (doubles); -1: the rows live in shared memory
+  int32_t smem_adj = 0;  // shared doubles needed (adjoint)
+  int32_t _pad2 = 0;
 };
 
 struct Packed2 {
@@ -237,6 +241,10 @@ struct Packed2 {
   // (kNT2H threads) tasks, with the largest shared memory of each launch
   std::vector<std::vector<int32_t>> levels, levels_h;
   std::vector<int32_t> level_smem, level_smem_adj, level_smem_h, level_smem_adj_h;
+  // tasks whose rows exceed shared memory (working rows in device scratch),
+  // per level: 128-thread (root) and 256-thread CTAs
+  std::vector<std::vector<int32_t>> levels_g, levels_gh;
+  int64_t scratch_doubles = 0;
   int64_t tops_doubles = 0, tab_doubles = 0, gout_doubles = 0;
   // gradient reduction: for every output j (3 NR + K + 1), the gout indices
   // that contribute, in a fixed order (CSR)
@@ -260,6 +268,9 @@ struct PackOptions2 {
   // together), up to max_width_root clades (their adjoint keeps six rows).
   int root_group = 16;
   int64_t max_width_root = 1536;
+  // tasks needing more shared doubles than this keep their working rows in
+  // device memory (L2-resident) instead
+  int64_t smem_limit_doubles = 227 * 1024 / 8;
   int target_j = 3;           // iterations per row the lane scheduler aims for
   bool keep_tables = false;
   bool adjoint = false;

@@ -237,6 +237,7 @@ struct KArgs2 {
   double* bartops;
   double* gout;
   double* logl;
+  double* scratch;  // working rows of the tasks too wide for shared memory
   int NR, K;
 };
 
@@ -595,10 +596,14 @@ __device__ __forceinline__ bool fwd_rows_dispatch(int j, const DEntry* __restric
 // ROOT: the launch of the top level, whose tasks are all root tasks; the other
 // launches hold no root task.  Separate instantiations keep the root-row
 // machinery out of the register budget of the branch kernels.
-template <bool TABLES, int NT, bool ROOT = false>
+// GLOBAL: the tasks of the launch keep their working rows in device memory
+// (A.scratch + T.scratch, L2-resident) because they do not fit in shared
+// memory; the code is otherwise the same.
+template <bool TABLES, int NT, bool ROOT = false, bool GLOBAL = false>
 __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restrict__ list) {
-  extern __shared__ double sm[];
+  extern __shared__ double smem_dyn[];
   const DTask& T = A.tasks[list[blockIdx.x]];
+  double* const sm = GLOBAL ? A.scratch + T.scratch : smem_dyn;
   const int k = T.node;
   const int4 mn = A.mnode[k];
   const int R = T.width;
@@ -776,10 +781,14 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
   // Row r reads table row r-1 from buffer (n-1-r) mod 3 (buffer i at Lb +
   // i·W2); the copies run two rows ahead, one commit group per row (empty
   // past row 1).
+  const bool gmem = T.scratch >= 0;  // rows in device memory: plain copies
   auto fetch = [&](int rr, double* dst) {
     if (rr >= 1) {
       const double* src = tab0 + (int64_t)(rr - 1) * R;
-      for (int c = tid; c < R; c += NT) cp_async8(dst + c, src + c);
+      if (gmem)
+        for (int c = tid; c < R; c += NT) dst[c] = src[c];
+      else
+        for (int c = tid; c < R; c += NT) cp_async8(dst + c, src + c);
     }
     cp_async_commit();
   };
@@ -885,10 +894,12 @@ __device__ __forceinline__ bool adj_rows_dispatch(int j, const DEntry* __restric
 // ROOT as for k_fwd2.  Four 128-thread CTAs per SM leave the adjoint its
 // ~120 registers: at five or six the spills cost more than the occupancy
 // gains (the rows are latency-bound, not FP64-bound).
-template <int NT, bool ROOT = false>
-__global__ void __launch_bounds__(NT, NT == 128 ? 4 : 2) k_adj2(const KArgs2 A, const int* __restrict__ list) {
-  extern __shared__ double sm[];
+template <int NT, bool ROOT = false, bool GLOBAL = false>
+__global__ void __launch_bounds__(NT, NT == 128 && !GLOBAL ? 4 : (GLOBAL ? 1 : 2))
+    k_adj2(const KArgs2 A, const int* __restrict__ list) {
+  extern __shared__ double smem_dyn[];
   const DTask& T = A.tasks[list[blockIdx.x]];
+  double* const sm = GLOBAL ? A.scratch + T.scratch : smem_dyn;
   const int k = T.node;
   const int4 mn = A.mnode[k];
   const int R = T.width;
@@ -1220,6 +1231,8 @@ struct SubBatch {
   std::vector<int> fam;  // global family index of each local family
   std::vector<int> lvl_off, lvl_n, lvlh_off, lvlh_n;
   std::vector<size_t> lvl_smem, lvl_smem_adj, lvlh_smem, lvlh_smem_adj;
+  std::vector<int> lvlg_off, lvlg_n, lvlgh_off, lvlgh_n;  // tasks with rows in device scratch
+  double* d_scratch = nullptr;
   std::vector<int64_t> fam_tab;
   std::vector<int32_t> fam_w, fam_col, fam_ncol;
   DTask* d_tasks = nullptr;
@@ -1241,7 +1254,7 @@ struct SubBatch {
   cudaEvent_t fork = nullptr, join = nullptr, done = nullptr;
   ~SubBatch() {
     free_all(device, {d_tasks, d_entries, d_meta, d_gmap, d_progs, d_lists, d_red_off, d_red_idx, d_tops, d_tabs,
-                      d_bartops, d_gout, d_gred},
+                      d_bartops, d_gout, d_gred, d_scratch},
              {});
     for (cudaEvent_t e : {fork, join, done})
       if (e) cudaEventDestroy(e);
@@ -1404,6 +1417,7 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
     opt.adjoint = adjoint;
     opt.keep_tables = keep;
     opt.global_ids = &ids;
+    opt.smem_limit_doubles = (flags & WG_BATCH_SCRATCH_ROWS) ? 0 : (int64_t)(ctx->smem_optin / sizeof(double));
     Packed2 P = pack_batch2(*m, cs, opt);
     if ((size_t)P.max_smem * sizeof(double) > ctx->smem_optin)
       throw Error(WG_ERANGE, "a task needs more shared memory than one CTA can hold");
@@ -1423,12 +1437,13 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
       b->fam_sub[ids[i]] = (int)b->subs.size();
       b->fam_local[ids[i]] = (int)i;
     }
-    if (!P.levels_h.empty() && !P.levels_h.back().empty())
+    if ((!P.levels_h.empty() && !P.levels_h.back().empty()) || (!P.levels_gh.empty() && !P.levels_gh.back().empty()))
       throw Error(WG_ESTATE, "internal: heavy task at the root level");
     for (size_t L = 0; L < P.levels.size(); ++L)
-      for (int t : P.levels[L])
-        if ((m->kind[P.tasks[t].node] == WG_NODE_ROOT) != (L + 1 == P.levels.size()))
-          throw Error(WG_ESTATE, "internal: root tasks must form the top level");
+      for (auto* lv : {&P.levels[L], &P.levels_g[L]})
+        for (int t : *lv)
+          if ((m->kind[P.tasks[t].node] == WG_NODE_ROOT) != (L + 1 == P.levels.size()))
+            throw Error(WG_ESTATE, "internal: root tasks must form the top level");
     std::vector<int> lists;
     for (size_t L = 0; L < P.levels.size(); ++L) {
       sb->lvl_off.push_back((int)lists.size());
@@ -1441,7 +1456,14 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
       sb->lvlh_smem.push_back((size_t)P.level_smem_h[L] * sizeof(double));
       sb->lvlh_smem_adj.push_back((size_t)P.level_smem_adj_h[L] * sizeof(double));
       lists.insert(lists.end(), P.levels_h[L].begin(), P.levels_h[L].end());
+      sb->lvlg_off.push_back((int)lists.size());
+      sb->lvlg_n.push_back((int)P.levels_g[L].size());
+      lists.insert(lists.end(), P.levels_g[L].begin(), P.levels_g[L].end());
+      sb->lvlgh_off.push_back((int)lists.size());
+      sb->lvlgh_n.push_back((int)P.levels_gh[L].size());
+      lists.insert(lists.end(), P.levels_gh[L].begin(), P.levels_gh[L].end());
     }
+    if (P.scratch_doubles > 0) sb->d_scratch = dalloc<double>(P.scratch_doubles, by);
     sb->d_tasks = dalloc<DTask>(P.tasks.size(), by);
     sb->d_entries = dalloc<DEntry>(P.entries.size(), by);
     sb->d_meta = dalloc<int>(P.meta.size(), by);
@@ -1504,6 +1526,7 @@ KArgs2 sub_args(const wg_batch* b, const SubBatch* sb) {
   A.bartops = sb->d_bartops;
   A.gout = sb->d_gout;
   A.logl = b->d_logl;
+  A.scratch = sb->d_scratch;
   A.NR = b->NR;
   A.K = b->K;
   return A;
@@ -1516,10 +1539,11 @@ void check_model(const B* b, const wg_model* m) {
 }
 
 // One level of one size class: heavy tasks on the class's second stream,
-// light ones on its first, joined before the next level.
+// light ones on its first, joined before the next level (each side also
+// launches its tasks whose rows live in device scratch).
 template <class Light, class Heavy>
 void run_level(SubBatch* sb, int L, Light light, Heavy heavy) {
-  const bool h = sb->lvlh_n[L] > 0, l = sb->lvl_n[L] > 0;
+  const bool h = sb->lvlh_n[L] + sb->lvlgh_n[L] > 0, l = sb->lvl_n[L] + sb->lvlg_n[L] > 0;
   if (h && l) {
     ck(cudaEventRecord(sb->fork, sb->s), "event");
     ck(cudaStreamWaitEvent(sb->s2, sb->fork, 0), "wait");
@@ -1594,18 +1618,36 @@ void record_sequence(wg_batch* b, bool grad, bool tables) {
       run_level(
           sb, L,
           [&](cudaStream_t st) {
-            ++nl;
-            const dim3 g(sb->lvl_n[L]);
+            const dim3 g(sb->lvl_n[L]), gg(sb->lvlg_n[L]);
             const size_t sm = sb->lvl_smem[L];
-            if (L == top && tables) k_fwd2<true, kNT2L, true><<<g, kNT2L, sm, st>>>(A, ll);
-            else if (L == top) k_fwd2<false, kNT2L, true><<<g, kNT2L, sm, st>>>(A, ll);
-            else if (tables) k_fwd2<true, kNT2L><<<g, kNT2L, sm, st>>>(A, ll);
-            else k_fwd2<false, kNT2L><<<g, kNT2L, sm, st>>>(A, ll);
+            const int* lg = sb->d_lists + sb->lvlg_off[L];
+            if (sb->lvl_n[L] > 0) {
+              ++nl;
+              if (L == top && tables) k_fwd2<true, kNT2L, true><<<g, kNT2L, sm, st>>>(A, ll);
+              else if (L == top) k_fwd2<false, kNT2L, true><<<g, kNT2L, sm, st>>>(A, ll);
+              else if (tables) k_fwd2<true, kNT2L><<<g, kNT2L, sm, st>>>(A, ll);
+              else k_fwd2<false, kNT2L><<<g, kNT2L, sm, st>>>(A, ll);
+            }
+            if (sb->lvlg_n[L] > 0) {
+              ++nl;
+              if (L == top && tables) k_fwd2<true, kNT2L, true, true><<<gg, kNT2L, 0, st>>>(A, lg);
+              else if (L == top) k_fwd2<false, kNT2L, true, true><<<gg, kNT2L, 0, st>>>(A, lg);
+              else if (tables) k_fwd2<true, kNT2L, false, true><<<gg, kNT2L, 0, st>>>(A, lg);
+              else k_fwd2<false, kNT2L, false, true><<<gg, kNT2L, 0, st>>>(A, lg);
+            }
           },
           [&](cudaStream_t st) {
-            ++nl;
-            if (tables) k_fwd2<true, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], st>>>(A, lh);
-            else k_fwd2<false, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], st>>>(A, lh);
+            const int* lgh = sb->d_lists + sb->lvlgh_off[L];
+            if (sb->lvlh_n[L] > 0) {
+              ++nl;
+              if (tables) k_fwd2<true, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], st>>>(A, lh);
+              else k_fwd2<false, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], st>>>(A, lh);
+            }
+            if (sb->lvlgh_n[L] > 0) {
+              ++nl;
+              if (tables) k_fwd2<true, kNT2H, false, true><<<sb->lvlgh_n[L], kNT2H, 0, st>>>(A, lgh);
+              else k_fwd2<false, kNT2H, false, true><<<sb->lvlgh_n[L], kNT2H, 0, st>>>(A, lgh);
+            }
           });
     }
   }
@@ -1624,13 +1666,28 @@ void record_sequence(wg_batch* b, bool grad, bool tables) {
         run_level(
             sb, L,
             [&](cudaStream_t st) {
-              ++nl;
-              if (L == top) k_adj2<kNT2L, true><<<sb->lvl_n[L], kNT2L, sb->lvl_smem_adj[L], st>>>(A, ll);
-              else k_adj2<kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem_adj[L], st>>>(A, ll);
+              const int* lg = sb->d_lists + sb->lvlg_off[L];
+              if (sb->lvl_n[L] > 0) {
+                ++nl;
+                if (L == top) k_adj2<kNT2L, true><<<sb->lvl_n[L], kNT2L, sb->lvl_smem_adj[L], st>>>(A, ll);
+                else k_adj2<kNT2L><<<sb->lvl_n[L], kNT2L, sb->lvl_smem_adj[L], st>>>(A, ll);
+              }
+              if (sb->lvlg_n[L] > 0) {
+                ++nl;
+                if (L == top) k_adj2<kNT2L, true, true><<<sb->lvlg_n[L], kNT2L, 0, st>>>(A, lg);
+                else k_adj2<kNT2L, false, true><<<sb->lvlg_n[L], kNT2L, 0, st>>>(A, lg);
+              }
             },
             [&](cudaStream_t st) {
-              ++nl;
-              k_adj2<kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem_adj[L], st>>>(A, lh);
+              const int* lgh = sb->d_lists + sb->lvlgh_off[L];
+              if (sb->lvlh_n[L] > 0) {
+                ++nl;
+                k_adj2<kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem_adj[L], st>>>(A, lh);
+              }
+              if (sb->lvlgh_n[L] > 0) {
+                ++nl;
+                k_adj2<kNT2H, false, true><<<sb->lvlgh_n[L], kNT2H, 0, st>>>(A, lgh);
+              }
             });
       }
       ++nl;
@@ -2037,6 +2094,13 @@ extern "C" int wg_logpdf_noalloc(wg_ctx* ctx, wg_model* m, wg_batch* b, double* 
       A.tabs = nullptr;
       off += sb->tops_doubles;
       for (int L = 0; L < (int)sb->lvl_n.size(); ++L) {
+        const bool top = L + 1 == (int)sb->lvl_n.size();
+        if (sb->lvlgh_n[L] > 0)
+          k_fwd2<false, kNT2H, false, true><<<sb->lvlgh_n[L], kNT2H, 0, s>>>(A, sb->d_lists + sb->lvlgh_off[L]);
+        if (sb->lvlg_n[L] > 0 && top)
+          k_fwd2<false, kNT2L, true, true><<<sb->lvlg_n[L], kNT2L, 0, s>>>(A, sb->d_lists + sb->lvlg_off[L]);
+        else if (sb->lvlg_n[L] > 0)
+          k_fwd2<false, kNT2L, false, true><<<sb->lvlg_n[L], kNT2L, 0, s>>>(A, sb->d_lists + sb->lvlg_off[L]);
         if (sb->lvlh_n[L] > 0)
           k_fwd2<false, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], s>>>(A, sb->d_lists + sb->lvlh_off[L]);
         if (sb->lvl_n[L] > 0 && L + 1 == (int)sb->lvl_n.size())

@@ -668,6 +668,8 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
   }
   P.levels.assign(H + 1, {});
   P.levels_h.assign(H + 1, {});
+  P.levels_g.assign(H + 1, {});
+  P.levels_gh.assign(H + 1, {});
   P.level_smem.assign(H + 1, 0);
   P.level_smem_adj.assign(H + 1, 0);
   P.level_smem_h.assign(H + 1, 0);
@@ -725,16 +727,19 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       T.node = k;
       T.nfam = nf;
       const double gops = group_ops[gi];
-      // the root row is a chain of small same-row levels: latency-bound, so
-      // root tasks stay in narrow CTAs that pack densely on the SMs
-      const int NT = (kind != WG_NODE_ROOT && gops > opt.heavy_ops) ? kNT2H : kNT2L;
-      T.nt = NT;
       std::vector<int> col(nf + 1, 0), cola(nf + 1, 0), colb(nf + 1, 0);
       for (int i = 0; i < nf; ++i) {
         col[i + 1] = col[i] + info[fams[i]].ncompat[k];
         if (ka >= 0) cola[i + 1] = cola[i] + info[fams[i]].ncompat[ka];
         if (kb >= 0) colb[i + 1] = colb[i] + info[fams[i]].ncompat[kb];
       }
+      // the root row is a chain of small same-row levels: latency-bound, so
+      // root tasks stay in narrow CTAs that pack densely on the SMs; rows too
+      // wide for shared memory take the wide CTAs
+      const int64_t W2est = std::max<int64_t>(col[nf], (int64_t)cola[nf] + colb[nf]);
+      const bool wide = (opt.adjoint ? 6 : 2) * W2est + 2 * m.nrow[k] > opt.smem_limit_doubles;
+      const int NT = (kind != WG_NODE_ROOT && (gops > opt.heavy_ops || wide)) ? kNT2H : kNT2L;
+      T.nt = NT;
       const int R = col[nf];
       if (R >= 32768) throw Error(WG_ERANGE, "task row wider than 32767 clades");
       T.width = R;
@@ -966,6 +971,15 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       }
       const int h = height[k];
       const bool heavy = NT == kNT2H;
+      T.smem_adj = opt.adjoint ? smem_adj : 0;
+      if (std::max(T.smem, T.smem_adj) > opt.smem_limit_doubles) {
+        // working rows in device memory, one region per task
+        T.scratch = P.scratch_doubles;
+        P.scratch_doubles += std::max(T.smem, T.smem_adj);
+        (heavy ? P.levels_gh : P.levels_g)[h].push_back((int32_t)P.tasks.size());
+        P.tasks.push_back(T);
+        continue;
+      }
       (heavy ? P.levels_h : P.levels)[h].push_back((int32_t)P.tasks.size());
       int& sf = (heavy ? P.level_smem_h : P.level_smem)[h];
       sf = std::max(sf, T.smem);
@@ -987,6 +1001,8 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
   };
   for (auto& L : P.levels) std::stable_sort(L.begin(), L.end(), by_cost);
   for (auto& L : P.levels_h) std::stable_sort(L.begin(), L.end(), by_cost);
+  for (auto& L : P.levels_g) std::stable_sort(L.begin(), L.end(), by_cost);
+  for (auto& L : P.levels_gh) std::stable_sort(L.begin(), L.end(), by_cost);
   P.red_off.assign(red.size() + 1, 0);
   for (size_t j = 0; j < red.size(); ++j) {
     P.red_off[j + 1] = P.red_off[j] + (int64_t)red[j].size();
