@@ -166,6 +166,16 @@ int wg_logpdf(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, double*
 int wg_logpdf_grad(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, double* total,
                    double* d_lam, double* d_mu, double* d_q, double* d_eta,
                    double* d_eps, double* d_phi, double* d_psi);
+/* Weighted form: total = sum_i weights[i] * per_family[i] - cond_scale *
+ * condition (terms with weight 0 dropped) and its gradient, the adjoint of
+ * family i seeded with weights[i] (weights: one per family, in batch order).
+ * The building block of MixtureModel (src/core.jl:66-75: weights = each
+ * family's posterior component weight, cond_scale = their sum) and ModelArray
+ * (src/core.jl:77-78: unconditioned, cond_scale = 0); the reference has no C
+ * counterpart. */
+int wg_logpdf_grad_weighted(wg_ctx* ctx, wg_model* m, wg_batch* b, const double* weights, double cond_scale,
+                            double* per_family, double* total, double* d_lam, double* d_mu, double* d_q,
+                            double* d_eta, double* d_eps, double* d_phi, double* d_psi);
 /* One family per launch: the plain per-family path (src/core.jl:39-43). */
 int wg_logpdf_plain(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, double* total);
 /* logpdf! (src/core.jl:29-37): also returns family i's DP tables.  out holds,

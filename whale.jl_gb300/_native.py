@@ -72,6 +72,8 @@ def _declare(L):
         "wg_batch_launches": (C.c_int, [vp, P_i32, P_i32]),
         "wg_logpdf": (C.c_int, [vp, vp, vp, P_dbl, P_dbl]),
         "wg_logpdf_grad": (C.c_int, [vp, vp, vp, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl]),
+        "wg_logpdf_grad_weighted": (C.c_int, [vp, vp, vp, P_dbl, C.c_double, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl,
+                                              P_dbl, P_dbl, P_dbl]),
         "wg_logpdf_plain": (C.c_int, [vp, vp, vp, P_dbl, P_dbl]),
         "wg_logpdf_noalloc": (C.c_int, [vp, vp, vp, P_dbl, P_dbl]),
         "wg_logpdf_tables": (C.c_int, [vp, vp, vp, i32, P_dbl, i64, P_i64, P_dbl]),

@@ -121,6 +121,24 @@ class Batch:
                                        N.dptr(dm), N.dptr(dq), N.C.byref(de), None, None, None))
         return tot.value, per, dl, dm, dq, de.value
 
+    def grad_nodes_weighted(self, wm: WhaleModel, weights, cond_scale: float):
+        """As grad_nodes for Σ_i weights[i]·log L_i - cond_scale·condition."""
+        if not self.grad:
+            raise ValueError("batch was created without gradient support")
+        wm.load()
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        if w.shape != (self.n,):
+            raise ValueError(f"need {self.n} family weights")
+        K = len(wm.order)
+        per = np.zeros(self.n)
+        dl, dm, dq = np.zeros(K), np.zeros(K), np.zeros(K)
+        de = N.dbl()
+        tot = N.dbl()
+        N.check(N.lib().wg_logpdf_grad_weighted(self.ctx.h, wm._struct.h, self.h, N.dptr(w), float(cond_scale),
+                                                N.dptr(per), N.C.byref(tot), N.dptr(dl), N.dptr(dm), N.dptr(dq),
+                                                N.C.byref(de), None, None, None))
+        return tot.value, per, dl, dm, dq, de.value
+
     def grad_tables(self, wm: WhaleModel):
         """Adjoints of the slice tables (ε, ϕ, ψ per row), q per node and η."""
         wm.load()
@@ -163,7 +181,14 @@ def get_batch(wm: WhaleModel, ccds: Sequence[CCD], grad: bool = False, tables: b
 
 def logpdf(wm: WhaleModel, x: Union[CCD, Sequence[CCD]]) -> float:
     """``logpdf(wm, x)``: a single CCD gives its unconditioned log L; a vector
-    gives Σ log L - N·condition (src/core.jl:39-43, :58-64)."""
+    gives Σ log L - N·condition (src/core.jl:39-43, :58-64).  A MixtureModel
+    or ModelArray dispatches to its own form (src/core.jl:66-79)."""
+    from . import mixture
+
+    if isinstance(wm, mixture.MixtureModel):
+        return mixture.logpdf(wm, x)
+    if isinstance(wm, mixture.ModelArray):
+        return mixture.modelarray_logpdf(wm, x)
     if isinstance(x, CCD):
         _, per = get_batch(wm, [x]).logpdf(wm, per_family=True)
         return float(per[0])
@@ -221,7 +246,15 @@ def logpdf_plain(wm: WhaleModel, xs: Sequence[CCD]):
 def logpdf_gradient(wm: WhaleModel, xs: Sequence[CCD]):
     """Σ log L - N·condition and its gradient w.r.t. the rates struct:
     for DLWGD a dict with 'λ', 'μ' (log-scale, by node id), 'q', 'η'; for
-    ConstantDLWGD scalars 'λ', 'μ', vector 'q' and 'η'."""
+    ConstantDLWGD scalars 'λ', 'μ', vector 'q' and 'η'.  A MixtureModel
+    returns (total, [gradient per component], d/d prior); a ModelArray
+    returns (total, [(model, gradient) per distinct model])."""
+    from . import mixture
+
+    if isinstance(wm, mixture.MixtureModel):
+        return mixture.logpdf_gradient(wm, xs)
+    if isinstance(wm, mixture.ModelArray):
+        return mixture.modelarray_logpdf_gradient(wm, xs)
     b = get_batch(wm, list(xs), grad=True)
     tot, per, dl, dm, dq, deta = b.grad_nodes(wm)
     return tot, map_gradient(wm, dl, dm, dq, deta)

@@ -238,6 +238,7 @@ struct KArgs2 {
   double* gout;
   double* logl;
   double* scratch;  // working rows of the tasks too wide for shared memory
+  const double* famw;  // adjoint seed weight per family (null: 1)
   int NR, K;
 };
 
@@ -942,7 +943,8 @@ __global__ void __launch_bounds__(NT, NT == 128 && !GLOBAL ? 4 : (GLOBAL ? 1 : 2
     const int2* fam = reinterpret_cast<const int2*>(A.meta) + T.fam;
     for (int f = tid; f < T.nfam; f += NT) {
       const double L = L0[fam[f].y];
-      bar[fam[f].y] = L > 0.0 ? 1.0 / L : 0.0;
+      const double w = A.famw ? A.famw[fam[f].x] : 1.0;  // ∂(Σ w log L)/∂L
+      bar[fam[f].y] = L > 0.0 ? w / L : 0.0;
     }
     __syncthreads();
     const double ca = A.params[3 * NR + A.K + 1], cb = A.params[3 * NR + A.K + 2];
@@ -1285,12 +1287,19 @@ struct wg_batch {
   int launches[2] = {0, 0};  // kernels per recorded sequence: [forward only, with gradient]
   std::vector<wg_ccd*> ccds;  // not owned; for the lazily built plain layout
   std::unique_ptr<PlainBatch> plain;
-  // captured launch sequences: [with gradient][with tables]
-  cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  // per-family adjoint weights (wg_logpdf_grad_weighted)
+  double* d_famw = nullptr;
+  double* h_famw = nullptr;
+  bool weighted_pending = false;
+  double cond_scale = 0.0;  // of the pending weighted evaluation
+  // captured launch sequences: [with gradient][with tables][weighted]
+  cudaGraphExec_t graph[2][2][2] = {};
   ~wg_batch() {
-    for (auto& g2 : graph)
-      for (auto& g : g2)
-        if (g) cudaGraphExecDestroy(g);
+    for (auto& g3 : graph)
+      for (auto& g2 : g3)
+        for (auto& g : g2)
+          if (g) cudaGraphExecDestroy(g);
+    if (ctx) free_all(ctx->device, {d_famw}, {h_famw});
     plain.reset();
     subs.clear();
     if (ctx) free_all(ctx->device, {d_mnode, d_rowoff, d_leafp, d_params, d_logl}, {h_params, h_logl, h_gred});
@@ -1527,6 +1536,7 @@ KArgs2 sub_args(const wg_batch* b, const SubBatch* sb) {
   A.gout = sb->d_gout;
   A.logl = b->d_logl;
   A.scratch = sb->d_scratch;
+  A.famw = nullptr;
   A.NR = b->NR;
   A.K = b->K;
   return A;
@@ -1596,13 +1606,15 @@ void stage_params(wg_batch* b, const wg_model* m) {
 
 // Every class's forward levels (and the reverse levels of the adjoint plus
 // its gradient reduction), forked from and joined back to the context stream.
-void record_sequence(wg_batch* b, bool grad, bool tables) {
+void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted) {
   wg_ctx* ctx = b->ctx;
   cudaStream_t s = ctx->stream;
   int& nl = b->launches[grad ? 1 : 0];
   nl = 0;
   ck(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(double) * (b->P + 2), cudaMemcpyHostToDevice, s),
      "params upload");
+  if (weighted)
+    ck(cudaMemcpyAsync(b->d_famw, b->h_famw, sizeof(double) * b->NF, cudaMemcpyHostToDevice, s), "weights upload");
   if (grad)
     for (auto& sb : b->subs)
       ck(cudaMemsetAsync(sb->d_gout, 0, sizeof(double) * (size_t)sb->gout_doubles, s), "memset");
@@ -1610,7 +1622,8 @@ void record_sequence(wg_batch* b, bool grad, bool tables) {
   fork_subs(b);
   for (auto& sbp : b->subs) {
     SubBatch* sb = sbp.get();
-    const KArgs2 A = sub_args(b, sb);
+    KArgs2 A = sub_args(b, sb);
+    A.famw = weighted ? b->d_famw : nullptr;
     const int top = (int)sb->lvl_n.size() - 1;  // the root level
     for (int L = 0; L < (int)sb->lvl_n.size(); ++L) {
       const int* ll = sb->d_lists + sb->lvl_off[L];
@@ -1658,7 +1671,8 @@ void record_sequence(wg_batch* b, bool grad, bool tables) {
     fork_subs(b);
     for (auto& sbp : b->subs) {
       SubBatch* sb = sbp.get();
-      const KArgs2 A = sub_args(b, sb);
+      KArgs2 A = sub_args(b, sb);
+      A.famw = weighted ? b->d_famw : nullptr;
       const int top = (int)sb->lvl_n.size() - 1;
       for (int L = (int)sb->lvl_n.size() - 1; L >= 0; --L) {
         const int* ll = sb->d_lists + sb->lvl_off[L];
@@ -1703,7 +1717,7 @@ void record_sequence(wg_batch* b, bool grad, bool tables) {
 
 // Stage the parameters on the host and replay the captured launch sequence
 // (captured into a CUDA graph on first use).
-void enqueue(wg_batch* b, const wg_model* m, bool grad) {
+void enqueue(wg_batch* b, const wg_model* m, bool grad, const double* weights = nullptr, double cond_scale = 0.0) {
   check_model(b, m);
   wg_ctx* ctx = b->ctx;
   ck(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -1713,13 +1727,24 @@ void enqueue(wg_batch* b, const wg_model* m, bool grad) {
   // the pinned parameter buffer is read by the previous launch's copy
   if (b->pending) ck(cudaStreamSynchronize(ctx->stream), "pending evaluation");
   stage_params(b, m);
+  const bool weighted = weights != nullptr;
+  if (weighted) {
+    if (!grad) throw Error(WG_EINVAL, "family weights apply to the gradient");
+    if (!b->d_famw) {
+      ck(cudaMalloc(&b->d_famw, sizeof(double) * b->NF), "cudaMalloc");
+      ck(cudaMallocHost(&b->h_famw, sizeof(double) * b->NF), "cudaMallocHost");
+    }
+    std::memcpy(b->h_famw, weights, sizeof(double) * b->NF);
+  }
+  b->weighted_pending = weighted;
+  b->cond_scale = weighted ? cond_scale : (double)b->NF;
   const bool tables = grad || (b->flags & WG_BATCH_TABLES);
-  cudaGraphExec_t& ge = b->graph[grad][tables];
+  cudaGraphExec_t& ge = b->graph[grad][tables][weighted];
   cudaStream_t s = ctx->stream;
   if (!ge) {
     ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
     try {
-      record_sequence(b, grad, tables);
+      record_sequence(b, grad, tables, weighted);
     } catch (...) {
       cudaGraph_t g = nullptr;
       cudaStreamEndCapture(s, &g);
@@ -1753,14 +1778,16 @@ void finish_timing(wg_ctx* ctx) {
 
 // Per-family log L, the conditioned total and (for a gradient evaluation) the
 // chain from the table adjoints to the rates, on the host.
+// Σ w_f log L_f - c·condition and its gradient; unweighted: w = 1, c = N
+// (src/core.jl:15, :58-64).
 void finish(const wg_model* m, int NF, const double* logl, const double* gred, bool grad, double* per_family,
             double* total, double* d_lam, double* d_mu, double* d_q, double* d_eta, double* d_eps, double* d_phi,
-            double* d_psi) {
-  // sum over families minus N * condition, ℓhood (src/core.jl:15, :58-64)
+            double* d_psi, const double* weights = nullptr, double cond_scale = -1.0) {
   double sum = 0.0;
-  for (int i = 0; i < NF; ++i) sum += logl[i];
+  for (int i = 0; i < NF; ++i) sum += weights ? (weights[i] != 0.0 ? weights[i] * logl[i] : 0.0) : logl[i];
   const double cond = model_condition(*m);
-  double tot = sum - NF * cond;
+  const double cs = cond_scale < 0 ? (double)NF : cond_scale;
+  double tot = sum - cs * cond;
   if (!std::isfinite(tot)) tot = -INFINITY;
   if (per_family) std::memcpy(per_family, logl, sizeof(double) * NF);
   if (total) *total = tot;
@@ -1769,7 +1796,7 @@ void finish(const wg_model* m, int NF, const double* logl, const double* gred, b
   std::vector<double> de(gred, gred + NR), dp(gred + NR, gred + 2 * NR), ds(gred + 2 * NR, gred + 3 * NR),
       dq(gred + 3 * NR, gred + 3 * NR + K);
   double deta = gred[3 * NR + K];
-  model_condition_vjp(*m, -(double)NF, de, deta);
+  model_condition_vjp(*m, -cs, de, deta);
   if (d_eps) std::memcpy(d_eps, de.data(), NR * sizeof(double));
   if (d_phi) std::memcpy(d_phi, dp.data(), NR * sizeof(double));
   if (d_psi) std::memcpy(d_psi, ds.data(), NR * sizeof(double));
@@ -1801,7 +1828,8 @@ void fetch(wg_batch* b, const wg_model* m, double* per_family, double* total, do
     for (size_t i = 1; i < b->subs.size(); ++i)
       for (int j = 0; j < b->P; ++j) gred[j] += b->h_gred[i * b->P + j];
   }
-  finish(m, b->NF, b->h_logl, gred.data(), grad, per_family, total, d_lam, d_mu, d_q, d_eta, d_eps, d_phi, d_psi);
+  finish(m, b->NF, b->h_logl, gred.data(), grad, per_family, total, d_lam, d_mu, d_q, d_eta, d_eps, d_phi, d_psi,
+         b->weighted_pending ? b->h_famw : nullptr, b->cond_scale);
 }
 
 void fetch_plain(PlainBatch* b, const wg_model* m, double* per_family, double* total) {
@@ -1958,6 +1986,17 @@ int wg_logpdf_grad(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, do
   WG_GUARD({
     if (!ctx || !m || !b || b->ctx != ctx) throw Error(WG_EINVAL, "wg_logpdf_grad: bad arguments");
     enqueue(b, m, true);
+    fetch(b, m, per_family, total, d_lam, d_mu, d_q, d_eta, d_eps, d_phi, d_psi);
+  });
+}
+
+int wg_logpdf_grad_weighted(wg_ctx* ctx, wg_model* m, wg_batch* b, const double* weights, double cond_scale,
+                            double* per_family, double* total, double* d_lam, double* d_mu, double* d_q,
+                            double* d_eta, double* d_eps, double* d_phi, double* d_psi) {
+  WG_GUARD({
+    if (!ctx || !m || !b || b->ctx != ctx || !weights) throw Error(WG_EINVAL, "wg_logpdf_grad_weighted: bad arguments");
+    if (!(cond_scale >= 0.0)) throw Error(WG_EINVAL, "wg_logpdf_grad_weighted: condition scale must be >= 0");
+    enqueue(b, m, true, weights, cond_scale);
     fetch(b, m, per_family, total, d_lam, d_mu, d_q, d_eta, d_eps, d_phi, d_psi);
   });
 }
