@@ -51,6 +51,7 @@ extern "C" {
 #define WG_COND_NONE 0
 #define WG_COND_ROOT 1
 #define WG_COND_NONEXTINCT 2
+#define WG_COND_NOWHERE 3  /* NowhereExtinctCondition (needs wg_model_set_rates; <= 22 leaves) */
 
 /* wg_batch_create flags */
 #define WG_BATCH_GRAD 1u   /* keep device space for the adjoint's DP tables */

@@ -23,7 +23,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libwhale_oracle.so")
 _lib = None
 
-COND = {"none": 0, "root": 1, "nonextinct": 2}
+COND = {"none": 0, "root": 1, "nonextinct": 2, "nowhere": 3}
 
 
 def build(force: bool = False) -> str:

@@ -147,7 +147,7 @@ static void postwalk(const Tree& t, int x, std::vector<int>& out) {
 // Model structure: src/model.jl:6-22 (Slices), :96-145 (WhaleModel ids/order),
 // :32-42 (setclade!), :54 (iswgd).
 // ---------------------------------------------------------------------------
-enum CondKind { COND_NONE = 0, COND_ROOT = 1, COND_NONEXTINCT = 2 };
+enum CondKind { COND_NONE = 0, COND_ROOT = 1, COND_NONEXTINCT = 2, COND_NOWHERE = 3 };
 
 struct MNode {
   int tn;            // index into Tree
@@ -593,11 +593,70 @@ static T logpdf_family(const Model& m, const Tables<T>& tb, const CCD& x, std::v
 // src/bdputil.jl:67
 template <class T> static T geompgf(const T& p, const T& s) { return p * s / (1.0 - (1.0 - p) * s); }
 
-// src/condition.jl:11-29
+// src/bdputil.jl:84-99: pgf of the linear birth-death process over time t
+// (critical form when isapprox(λ, μ, atol=1e-6))
 template <class T>
-static T condition(const Model& m, const Tables<T>& tb) {
+static T bdp_pgf(const T& λ, const T& μ, double t, const T& s) {
+  if (std::fabs(val(λ) - val(μ)) <= 1e-6)
+    return (1.0 - (λ * t - 1.0) * (s - 1.0)) / (1.0 - λ * t * (s - 1.0));
+  T ρ = exp((μ - λ) * t);
+  return (ρ * (λ * s - μ) - μ * (s - 1.0)) / (ρ * (λ * s - μ) - λ * (s - 1.0));
+}
+
+// src/bdputil.jl:114-135 (treepgf_allbinary and its inclusion-exclusion
+// signs): the joint pgf of the leaf counts at every binary argument, the
+// first child's index varying fastest, with the matching signs; a WGD node
+// applies wgdpgf (src/bdputil.jl:104) before its branch, the root the
+// geometric pgf of η.
+template <class T>
+static void treepgf_allbinary(const Model& m, const Rates<T>& r, int k, std::vector<T>& v, std::vector<double>& sg) {
+  const MNode& n = m.order[k];
+  const Theta<T> th = getθ(m, r, k);
+  const double t = m.tree.n[n.tn].dist;
+  std::vector<T> x;
+  if (n.leaf) {
+    x = {T(0.0), T(1.0)};
+    sg = {1.0, -1.0};
+  } else {
+    x = {T(1.0)};
+    sg = {1.0};
+    for (int c : n.ch) {
+      std::vector<T> vc;
+      std::vector<double> sc;
+      treepgf_allbinary(m, r, c, vc, sc);
+      std::vector<T> nx;
+      std::vector<double> ns;
+      for (size_t j = 0; j < vc.size(); ++j)
+        for (size_t i = 0; i < x.size(); ++i) {
+          nx.push_back(x[i] * vc[j]);
+          ns.push_back(sg[i] * sc[j]);
+        }
+      x.swap(nx);
+      sg.swap(ns);
+    }
+  }
+  v.resize(x.size());
+  for (size_t i = 0; i < x.size(); ++i) {
+    T y = n.wgd ? x[i] * (1.0 - th.q + x[i] * th.q) : x[i];
+    v[i] = n.root ? geompgf(th.eta, y) : bdp_pgf(th.lam, th.mu, t, y);
+  }
+}
+
+// src/condition.jl:11-36
+template <class T>
+static T condition(const Model& m, const Tables<T>& tb, const Rates<T>* rates = nullptr) {
   int r = (int)m.order.size() - 1;
   if (m.cond == COND_NONE) return T(0.0);
+  if (m.cond == COND_NOWHERE) {
+    if (!rates) throw std::runtime_error("NowhereExtinctCondition needs the rates");
+    std::vector<T> v;
+    std::vector<double> sg;
+    treepgf_allbinary(m, *rates, r, v, sg);
+    T acc(0.0);
+    for (size_t i = 0; i + 1 < v.size(); ++i) acc = acc + v[i] * sg[i];
+    T c = 1.0 - acc;
+    return (val(c) > 0 && val(c) < 1) ? log(c) : T(-INFINITY);
+  }
   T η = tb.eta;
   if (m.cond == COND_NONEXTINCT) return log(1.0 - geompgf(η, tb.eps[r].back()));
   int f = m.order[r].ch[0], g = m.order[r].ch[1];
@@ -684,7 +743,7 @@ double orc_logpdf(void* mp, int kind, const double* lam, int nlam, const double*
   for (int i = 0; i < nccd; ++i) ll[i] = logpdf_family(*m, tb, *(CCD*)ccds[i], (std::vector<Tab<double>>*)nullptr);
   double s = 0.0;
   for (int i = 0; i < nccd; ++i) { s += ll[i]; if (per_family) per_family[i] = ll[i]; }
-  s = s - nccd * condition(*m, tb);
+  s = s - nccd * condition(*m, tb, &r);
   return std::isfinite(s) ? s : -INFINITY;
 }
 
@@ -692,7 +751,7 @@ double orc_condition(void* mp, int kind, const double* lam, int nlam, const doub
                      const double* q, int nq, double eta, const double* p, int np) {
   Model* m = (Model*)mp;
   Rates<double> r = make_rates(kind, lam, nlam, mu, nmu, q, nq, eta, p, np);
-  return condition(*m, setmodel(*m, r));
+  return condition(*m, setmodel(*m, r), &r);
 }
 
 // Slice tables for inspection: eps/phi/psi concatenated over order positions.
@@ -748,7 +807,7 @@ double orc_gradient(void* mp, int kind, const double* lam, int nlam, const doubl
     for (int i = 0; i < nccd; ++i) ll[i] = logpdf_family(*m, tb, *(CCD*)ccds[i], (std::vector<Tab<D>>*)nullptr);
     D s(0.0);
     for (int i = 0; i < nccd; ++i) s += ll[i];
-    s = s - (double)nccd * condition(*m, tb);
+    s = s - (double)nccd * condition(*m, tb, &r);
     total = std::isfinite(s.v) ? s.v : -INFINITY;
     for (int k = 0; k < C && c0 + k < P; ++k) grad[c0 + k] = s.d[k];
   }

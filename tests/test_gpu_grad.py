@@ -101,3 +101,20 @@ def test_gradient_deterministic(W, ex1_tree, ex1_files):
     a = W.gradient(wm, ccds)
     b = W.gradient(wm, ccds)
     assert np.array_equal(a, b)
+
+
+def test_gradient_nowhere_extinct_condition(W, O, ex1_tree, ex1_files):
+    # NowhereExtinctCondition (src/condition.jl:31-36) depends on the rates
+    # directly; its gradient joins the DP's through the host chain rule
+    t = W.readnw(ex1_tree)
+    rng = np.random.default_rng(9)
+    lam, mu = rng.normal(-0.6, 0.4, 17), rng.normal(-0.8, 0.4, 17)
+    wm = W.WhaleModel(W.DLWGD(λ=lam, μ=mu, q=[0.25, 0.5], η=0.72), t, 0.05,
+                      condition=W.NowhereExtinctCondition(t))
+    ccds = W.read_ale(os.path.dirname(ex1_files[0]), wm)
+    tot, gd = W.logpdf_gradient(wm, ccds)
+    g = np.concatenate([gd["λ"], gd["μ"], gd["q"], [gd["η"]]])
+    om = O.OracleModel(ex1_tree, 0.05, condition="nowhere")
+    otot, og = om.gradient(O.read_ale_files(om, ex1_files), lam, mu, q=[0.25, 0.5], eta=0.72)
+    assert tot == pytest.approx(otot, rel=1e-10)
+    assert _close(g, og) <= GREL

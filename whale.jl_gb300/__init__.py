@@ -15,14 +15,16 @@ from .ccd import CCD, parse_ale_text, read_ale
 from .core import (Batch, Context, default_context, get_batch, gradient, logpdf, logpdf_gradient, logpdf_inplace,
                    logpdf_plain, loglikelihood, map_gradient)
 from .mixture import MixtureModel, ModelArray
-from .model import (ConstantDLWGD, DLWGD, NoCondition, NonExtinctCondition, RootCondition, WhaleModel, condition)
+from .model import (ConstantDLWGD, DLWGD, NoCondition, NonExtinctCondition, NowhereExtinctCondition, RootCondition,
+                    WhaleModel, condition)
 from .newick import (EXTREE, Node, addbranchwgds, copytree, extree, getlca, getleaves, getroot, insertnode, nwstr,
                      postwalk, prewalk, readnw)
 
 logpdf_ = logpdf_inplace
 
 __all__ = [
-    "WhaleModel", "DLWGD", "ConstantDLWGD", "RootCondition", "NonExtinctCondition", "NoCondition", "condition",
+    "WhaleModel", "DLWGD", "ConstantDLWGD", "RootCondition", "NonExtinctCondition", "NoCondition",
+    "NowhereExtinctCondition", "condition",
     "CCD", "read_ale", "parse_ale_text", "logpdf", "logpdf_inplace", "logpdf_", "loglikelihood", "gradient",
     "logpdf_gradient", "logpdf_plain", "map_gradient", "Batch", "Context", "default_context", "get_batch",
     "readnw", "nwstr", "insertnode", "getlca", "getleaves", "getroot", "postwalk", "prewalk", "extree", "EXTREE",

@@ -13,7 +13,7 @@ from . import build as _build
 WG_OK = 0
 WG_EINVAL, WG_EPARSE, WG_ECUDA, WG_ENOMEM, WG_ESTATE, WG_ERANGE = -1, -2, -3, -4, -5, -6
 NODE_LEAF, NODE_INTERNAL, NODE_WGD, NODE_ROOT = 0, 1, 2, 3
-COND_NONE, COND_ROOT, COND_NONEXTINCT = 0, 1, 2
+COND_NONE, COND_ROOT, COND_NONEXTINCT, COND_NOWHERE = 0, 1, 2, 3
 BATCH_GRAD, BATCH_TABLES, BATCH_SCRATCH_ROWS = 1, 2, 4
 SYNTH_WALK, SYNTH_PUSH = 1, 2
 

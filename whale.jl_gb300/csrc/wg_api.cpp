@@ -30,7 +30,7 @@ int wg_model_create(int32_t n_nodes, const int32_t* kind, const int32_t* child0,
     if (!out || n_nodes < 3 || !kind || !child0 || !child1 || !nrow || !slice_len || !leaf_p || !clade_offsets ||
         !clade_species)
       throw wg::Error(WG_EINVAL, "wg_model_create: bad arguments");
-    if (condition < WG_COND_NONE || condition > WG_COND_NONEXTINCT)
+    if (condition < WG_COND_NONE || condition > WG_COND_NOWHERE)
       throw wg::Error(WG_EINVAL, "wg_model_create: unknown condition");
     auto* m = new wg_model();
     m->K = n_nodes;

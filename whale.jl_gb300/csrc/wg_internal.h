@@ -49,6 +49,11 @@ double model_condition(const Model& m);
 // Adjoint of the condition w.r.t. the tables: adds -scale * d cond to the
 // adjoints of the top ε of the root's children / root and to d_eta.
 void model_condition_vjp(const Model& m, double scale, std::vector<double>& d_eps, double& d_eta);
+// NowhereExtinctCondition depends on the rates directly: adds scale * d cond
+// to the adjoints of the per-node natural rates λ, μ, q and to d_eta (no-op
+// for the other conditions).
+void model_condition_rates_vjp(const Model& m, double scale, std::vector<double>& d_lam, std::vector<double>& d_mu,
+                               std::vector<double>& d_q, double& d_eta);
 // Adjoint of setmodel!: given adjoints of every table entry (eps/phi/psi per
 // row) and of q per node, accumulates adjoints of lam, mu, q, p per node.
 void model_tables_vjp(const Model& m, std::vector<double> d_eps, const std::vector<double>& d_phi,

@@ -1800,13 +1800,15 @@ void finish(const wg_model* m, int NF, const double* logl, const double* gred, b
   if (d_eps) std::memcpy(d_eps, de.data(), NR * sizeof(double));
   if (d_phi) std::memcpy(d_phi, dp.data(), NR * sizeof(double));
   if (d_psi) std::memcpy(d_psi, ds.data(), NR * sizeof(double));
-  if (d_eta) *d_eta = deta;
-  if (m->from_rates && (d_lam || d_mu || d_q)) {
+  if (m->from_rates) {
     std::vector<double> dl, dm, dpp;
-    model_tables_vjp(*m, de, dp, ds, dl, dm, dq, dpp);
+    if (d_lam || d_mu || d_q) model_tables_vjp(*m, de, dp, ds, dl, dm, dq, dpp);
+    // a condition on the rates themselves (NowhereExtinct) adds its own adjoints
+    model_condition_rates_vjp(*m, -cs, dl, dm, dq, deta);
     if (d_lam) std::memcpy(d_lam, dl.data(), K * sizeof(double));
     if (d_mu) std::memcpy(d_mu, dm.data(), K * sizeof(double));
   }
+  if (d_eta) *d_eta = deta;
   if (d_q) std::memcpy(d_q, dq.data(), K * sizeof(double));
 }
 

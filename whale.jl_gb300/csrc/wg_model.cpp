@@ -6,7 +6,10 @@
 //   getα, _ϵ, _ϕ, _ψ                             src/bdputil.jl:6-11
 //   geompgf                                      src/bdputil.jl:67
 //   condition (Root / NonExtinct / No)           src/condition.jl:11-29
+//   NowhereExtinctCondition                      src/condition.jl:31-36
+//   pgf of the linear BDP, treepgf_allbinary     src/bdputil.jl:84-135
 #include <cmath>
+#include <vector>
 
 #include "wg_internal.h"
 
@@ -41,6 +44,133 @@ inline void alpha_grad(double lam, double mu, double t, double& da_dlam, double&
 }
 
 inline double geompgf(double p, double s) { return p * s / (1.0 - (1.0 - p) * s); }
+
+// pgf of the linear birth-death process over time t at s (src/bdputil.jl:
+// 84-99; critical form when |λ - μ| <= 1e-6) with its partials in s, λ, μ.
+inline double bdp_pgf(double lam, double mu, double t, double s, double& ds, double& dlam, double& dmu) {
+  if (critical(lam, mu)) {
+    const double u = s - 1.0, lt = lam * t;
+    const double num = 1.0 - (lt - 1.0) * u, den = 1.0 - lt * u;
+    ds = (-(lt - 1.0) * den + num * lt) / (den * den);
+    dlam = (-t * u * den + num * t * u) / (den * den);
+    dmu = 0.0;
+    return num / den;
+  }
+  const double rho = std::exp((mu - lam) * t);
+  const double a = lam * s - mu, u = s - 1.0;
+  const double num = rho * a - mu * u, den = rho * a - lam * u;
+  const double drho_dl = -t * rho, drho_dm = t * rho;
+  const double dnum_ds = rho * lam - mu, dden_ds = rho * lam - lam;
+  const double dnum_dl = drho_dl * a + rho * s, dden_dl = drho_dl * a + rho * s - u;
+  const double dnum_dm = drho_dm * a - rho - u, dden_dm = drho_dm * a - rho;
+  ds = (dnum_ds * den - num * dden_ds) / (den * den);
+  dlam = (dnum_dl * den - num * dden_dl) / (den * den);
+  dmu = (dnum_dm * den - num * dden_dm) / (den * den);
+  return num / den;
+}
+
+// NowhereExtinctCondition: log(1 - Σ_{k<last} P_k s_k) over the joint pgf P
+// of the leaf counts at every binary argument and its inclusion-exclusion
+// signs s (treepgf_allbinary, src/bdputil.jl:114-135; the first child's
+// index varies fastest).  With grad, reverse-mode adjoints of the per-node
+// natural rates λ, μ, q and of η are added, scaled by `scale`.
+constexpr int kNowhereMaxLeaves = 22;
+
+double nowhere_condition(const Model& m, bool grad, double scale, std::vector<double>* d_lam,
+                         std::vector<double>* d_mu, std::vector<double>* d_q, double* d_eta) {
+  if (!m.from_rates) throw Error(WG_ESTATE, "NowhereExtinctCondition needs the model's rates (wg_model_set_rates)");
+  const int K = m.K, r = K - 1;
+  int nleaf = 0;
+  for (int k = 0; k < K; ++k) nleaf += m.kind[k] == WG_NODE_LEAF;
+  if (nleaf > kNowhereMaxLeaves)
+    throw Error(WG_ERANGE, "NowhereExtinctCondition over more than 22 leaves (2^leaves pgf terms)");
+  // forward: x_k (product of the children's outputs; leaves: [0, 1]) and v_k
+  std::vector<std::vector<double>> x(K), v(K), sg(K);
+  for (int k = 0; k < K; ++k) {  // children precede parents in the model order
+    if (m.kind[k] == WG_NODE_LEAF) {
+      x[k] = {0.0, 1.0};
+      sg[k] = {1.0, -1.0};
+    } else {
+      x[k] = {1.0};
+      sg[k] = {1.0};
+      for (int c : {m.ch0[k], m.ch1[k]}) {
+        if (c < 0) continue;
+        std::vector<double> nx, ns;
+        nx.reserve(x[k].size() * v[c].size());
+        ns.reserve(nx.capacity());
+        for (size_t j = 0; j < v[c].size(); ++j)
+          for (size_t i = 0; i < x[k].size(); ++i) {
+            nx.push_back(x[k][i] * v[c][j]);
+            ns.push_back(sg[k][i] * sg[c][j]);
+          }
+        x[k].swap(nx);
+        sg[k].swap(ns);
+      }
+    }
+    const bool wgd = m.kind[k] == WG_NODE_WGD;
+    const double qk = wgd ? m.q[k] : 0.0, t = m.slice_len[k] * (m.nrow[k] - 1);
+    v[k].resize(x[k].size());
+    for (size_t i = 0; i < x[k].size(); ++i) {
+      const double y = wgd ? x[k][i] * (1.0 - qk + x[k][i] * qk) : x[k][i];
+      double ds, dl, dm;
+      v[k][i] = k == r ? geompgf(m.eta, y) : bdp_pgf(m.lam[k], m.mu[k], t, y, ds, dl, dm);
+    }
+  }
+  double acc = 0.0;
+  for (size_t i = 0; i + 1 < v[r].size(); ++i) acc += v[r][i] * sg[r][i];
+  const double c = 1.0 - acc;
+  const bool ok = c > 0.0 && c < 1.0;
+  const double val = ok ? std::log(c) : -INFINITY;
+  if (!grad || !ok) return val;
+  // reverse: bar_v of each node, parents before children
+  std::vector<std::vector<double>> bv(K);
+  bv[r].assign(v[r].size(), 0.0);
+  for (size_t i = 0; i + 1 < v[r].size(); ++i) bv[r][i] = -sg[r][i] / c;
+  for (int k = r; k >= 0; --k) {
+    if (bv[k].empty()) continue;
+    const bool wgd = m.kind[k] == WG_NODE_WGD;
+    const double qk = wgd ? m.q[k] : 0.0, t = m.slice_len[k] * (m.nrow[k] - 1);
+    std::vector<double> bx(x[k].size());
+    for (size_t i = 0; i < x[k].size(); ++i) {
+      const double xi = x[k][i];
+      const double y = wgd ? xi * (1.0 - qk + xi * qk) : xi;
+      double dvdy;
+      if (k == r) {
+        const double d = 1.0 - (1.0 - m.eta) * y;
+        dvdy = m.eta / (d * d);
+        *d_eta += scale * bv[k][i] * (y * (1.0 - y) / (d * d));
+      } else {
+        double dl, dm;
+        bdp_pgf(m.lam[k], m.mu[k], t, y, dvdy, dl, dm);
+        (*d_lam)[k] += scale * bv[k][i] * dl;
+        (*d_mu)[k] += scale * bv[k][i] * dm;
+      }
+      const double by = bv[k][i] * dvdy;
+      if (wgd) {
+        (*d_q)[k] += scale * by * (xi * xi - xi);
+        bx[i] = by * (1.0 - qk + 2.0 * xi * qk);
+      } else {
+        bx[i] = by;
+      }
+    }
+    if (m.kind[k] == WG_NODE_LEAF) continue;
+    const int c0 = m.ch0[k], c1 = m.ch1[k];
+    if (c1 < 0) {
+      bv[c0] = bx;  // a WGD node's only child
+      continue;
+    }
+    const size_t n0 = v[c0].size(), n1 = v[c1].size();
+    bv[c0].assign(n0, 0.0);
+    bv[c1].assign(n1, 0.0);
+    for (size_t j = 0; j < n1; ++j)
+      for (size_t i = 0; i < n0; ++i) {
+        const double b = bx[i + n0 * j];
+        bv[c0][i] += b * v[c1][j];
+        bv[c1][j] += b * v[c0][i];
+      }
+  }
+  return val;
+}
 
 }  // namespace
 
@@ -83,6 +213,8 @@ double model_condition(const Model& m) {
   switch (m.cond) {
     case WG_COND_NONE:
       return 0.0;
+    case WG_COND_NOWHERE:
+      return nowhere_condition(m, false, 0.0, nullptr, nullptr, nullptr, nullptr);
     case WG_COND_NONEXTINCT:
       return std::log(1.0 - geompgf(m.eta, m.eps_top(r)));
     default: {
@@ -95,13 +227,22 @@ double model_condition(const Model& m) {
   }
 }
 
+void model_condition_rates_vjp(const Model& m, double scale, std::vector<double>& d_lam, std::vector<double>& d_mu,
+                               std::vector<double>& d_q, double& d_eta) {
+  if (m.cond != WG_COND_NOWHERE) return;
+  d_lam.resize(m.K, 0.0);
+  d_mu.resize(m.K, 0.0);
+  d_q.resize(m.K, 0.0);
+  nowhere_condition(m, true, scale, &d_lam, &d_mu, &d_q, &d_eta);
+}
+
 void model_condition_vjp(const Model& m, double scale, std::vector<double>& d_eps, double& d_eta) {
   const int r = m.K - 1;
   const double eta = m.eta;
   auto g_s = [&](double s) { const double d = 1.0 - (1.0 - eta) * s; return eta / (d * d); };
   auto g_eta = [&](double s) { const double d = 1.0 - (1.0 - eta) * s; return s * (1.0 - s) / (d * d); };
   auto top = [&](int k) { return m.row_off[k] + m.nrow[k] - 1; };
-  if (m.cond == WG_COND_NONE) return;
+  if (m.cond == WG_COND_NONE || m.cond == WG_COND_NOWHERE) return;  // the latter: model_condition_rates_vjp
   if (m.cond == WG_COND_NONEXTINCT) {
     const double s = m.eps_top(r);
     const double P = 1.0 - geompgf(eta, s);

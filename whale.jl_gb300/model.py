@@ -42,6 +42,21 @@ class NoCondition(SamplingCondition):
     code = N.COND_NONE
 
 
+class NowhereExtinctCondition(SamplingCondition):
+    """Probability that every leaf keeps a copy (src/condition.jl:5-9, :31-36):
+    inclusion-exclusion over the joint pgf of the leaf counts at all 2^L
+    binary arguments (src/bdputil.jl:114-135), computed by the library with
+    its gradient on the rates.  ``NowhereExtinctCondition(tree)`` as in the
+    reference; the signs are implied by the tree, so the argument is only
+    checked (at most 22 leaves)."""
+
+    code = N.COND_NOWHERE
+
+    def __init__(self, tree=None):
+        if tree is not None and len(getleaves(tree)) > 22:
+            raise ValueError("NowhereExtinctCondition over more than 22 leaves (2^leaves pgf terms)")
+
+
 # ---------------------------------------------------------------- rates
 def _vec(x) -> np.ndarray:
     return np.asarray(x if x is not None else [], dtype=np.float64).reshape(-1).copy()
