@@ -202,6 +202,19 @@ int wg_logpdf_tables(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t family, doub
  * host threads, two contexts on one device) race on it. */
 int wg_logpdf_noalloc(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, double* total);
 
+/* backtrack (src/track.jl:180-488): samples n_samples reconciled gene trees
+ * of family i from its DP tables (the batch must have WG_BATCH_TABLES; the
+ * batch is evaluated first, as logpdf! then backtrack).  out receives one
+ * extended-Newick line per tree, NUL-terminated: nodes carry
+ * [&&NHX:label=<speciation|duplication|wgd|wgdloss|sploss|loss>:node=<model
+ * order position>:clade=<0-based clade, -1 for a loss>:slice=<t>], leaves the
+ * gene name (or "loss"), branch lengths from the reference's node heights.
+ * The same seed gives the same trees; *needed = bytes including the NUL (call
+ * with out == NULL to query).  Randomness is this library's xoshiro256**
+ * stream, not Julia's: trees match the reference in distribution. */
+int wg_backtrack(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t family, int32_t n_samples, uint64_t seed, char* out,
+                 int64_t cap, int64_t* needed);
+
 /* Asynchronous pair for device-side timing: enqueue the evaluation on the
  * context stream (inputs already resident), then fetch the results (this
  * synchronises).  with_grad selects the adjoint. */

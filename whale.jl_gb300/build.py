@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libwhalegpu.so")
 
-CXX_SRCS = ["wg_api.cpp", "wg_model.cpp", "wg_ccd.cpp", "wg_pack.cpp", "wg_synth.cpp"]
+CXX_SRCS = ["wg_api.cpp", "wg_model.cpp", "wg_ccd.cpp", "wg_pack.cpp", "wg_synth.cpp", "wg_track.cpp"]
 CU_SRCS = ["wg_kernels.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

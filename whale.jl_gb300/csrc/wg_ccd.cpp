@@ -232,6 +232,7 @@ CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& nam
     auto bi = bip.find(k);
     if (bi == bip.end()) throw Error(WG_EPARSE, "ALE: clade without a Bip count");
     c->nleaves.push_back((int)ord[i].first);
+    c->leaf_name.push_back(ord[i].first == 1 ? leafname.at(*set_id[k].begin()) : std::string());
     c->counts.push_back(bi->second);
     auto di = dip.find(k);
     if (di == dip.end() && ord[i].first > 1) throw Error(WG_EPARSE, "ALE: clade without Dip counts");

@@ -73,6 +73,7 @@ struct CCD {
   std::vector<int> sp_off, sp;           // species ids per clade (CSR)
   std::vector<int> split_off, g1, g2;    // splits per clade (CSR), 0-based clade ids
   std::vector<double> p;                 // Dip / Bip
+  std::vector<std::string> leaf_name;    // gene name of each single-gene clade ("" otherwise)
 };
 
 CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& names,
@@ -283,6 +284,14 @@ struct PackOptions2 {
 };
 
 Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const PackOptions2& opt);
+
+// For every node (model order) and clade: the clade's column among the
+// node's compatible clades (ascending clade id), -1 if incompatible.
+std::vector<std::vector<int>> compat_columns(const Model& m, const CCD& c);
+
+// Samples n reconciled trees of a family from its DP tables (the layout of
+// wg_logpdf_tables); one extended-Newick line per tree.
+std::string backtrack_family(const Model& m, const CCD& c, const double* tables, int n_samples, uint64_t seed);
 
 }  // namespace wg
 

@@ -2056,6 +2056,25 @@ int wg_logpdf_tables(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t family, doub
   });
 }
 
+int wg_backtrack(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t family, int32_t n_samples, uint64_t seed, char* out,
+                 int64_t cap, int64_t* needed) {
+  WG_GUARD({
+    if (!ctx || !m || !b || b->ctx != ctx || n_samples < 0) throw Error(WG_EINVAL, "wg_backtrack: bad arguments");
+    if (family < 0 || family >= b->NF) throw Error(WG_EINVAL, "family index out of range");
+    int64_t need = 0;
+    int rc = wg_logpdf_tables(ctx, m, b, family, nullptr, 0, &need, nullptr);
+    if (rc != WG_OK) throw Error(rc, wg_last_error());
+    std::vector<double> tab((size_t)std::max<int64_t>(need, 1));
+    rc = wg_logpdf_tables(ctx, m, b, family, tab.data(), need, &need, nullptr);
+    if (rc != WG_OK) throw Error(rc, wg_last_error());
+    const std::string text = backtrack_family(*m, *b->ccds[family], tab.data(), n_samples, seed);
+    if (needed) *needed = (int64_t)text.size() + 1;
+    if (!out) return WG_OK;
+    if (cap < (int64_t)text.size() + 1) throw Error(WG_ERANGE, "output buffer too small");
+    std::memcpy(out, text.c_str(), text.size() + 1);
+  });
+}
+
 int wg_enqueue(wg_ctx* ctx, wg_model* m, wg_batch* b, int with_grad) {
   WG_GUARD({
     if (!ctx || !m || !b || b->ctx != ctx) throw Error(WG_EINVAL, "wg_enqueue: bad arguments");

@@ -633,6 +633,12 @@ DProg2 schedule2(std::vector<Item>& items, int ntmax, int target_j, std::vector<
 
 }  // namespace
 
+std::vector<std::vector<int>> compat_columns(const Model& m, const CCD& c) {
+  FamInfo fi;
+  compat_of(m, c, fi, true);
+  return fi.idx;
+}
+
 Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const PackOptions2& opt) {
   Packed2 P;
   const int K = m.K;
