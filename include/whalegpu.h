@@ -214,6 +214,11 @@ int wg_logpdf_noalloc(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family,
  * stream, not Julia's: trees match the reference in distribution. */
 int wg_backtrack(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t family, int32_t n_samples, uint64_t seed, char* out,
                  int64_t cap, int64_t* needed);
+/* The same sampling from DP tables the caller already holds (host only, no
+ * device): tables in the wg_logpdf_tables layout for model m (its slice
+ * tables set) and CCD c; n_tables = their length. */
+int wg_backtrack_tables(const wg_model* m, const wg_ccd* c, const double* tables, int64_t n_tables, int32_t n_samples,
+                        uint64_t seed, char* out, int64_t cap, int64_t* needed);
 
 /* Asynchronous pair for device-side timing: enqueue the evaluation on the
  * context stream (inputs already resident), then fetch the results (this

@@ -1,0 +1,75 @@
+"""Backtracking on the host from the oracle's own DP tables (no GPU): valid
+reconciliations, and the root's first event drawn with the probabilities of
+the root recursion's terms (src/core.jl:130-158, src/track.jl:233-250,
+359-401) within 4 standard errors over 4,000 trees."""
+import numpy as np
+import pytest
+
+from test_gpu_backtrack import _genes
+
+
+def _setting(W, O):
+    from whale_gb300 import synth
+
+    wl = synth.config0(seed=8, n_families=6)
+    wm = wl.model
+    ccds = wl.ccds()
+    i = max(range(len(ccds)), key=lambda j: ccds[j].n_clades)
+    om = O.OracleModel(W.nwstr(wm.tree), wm.Δt)
+    oc = O.OracleCCD(om, wl.ale[i])
+    r = wm.rates
+    tab = om.family_tables(oc, [r.λ], [r.μ], q=r.q, eta=r.η, kind="ConstantDLWGD")
+    return wl, wm, ccds[i], i, om, tab
+
+
+def test_host_backtracking_from_oracle_tables(W, O):
+    from whale_gb300.track import backtrack_tables
+
+    wl, wm, ccd, i, om, tab = _setting(W, O)
+    r = wm.rates
+    trees = backtrack_tables(wm, ccd, tab, n=4000, seed=99)
+    genes = _genes(wl.ale[i])
+    for tr in trees[:300]:
+        leaves = [n for n in tr.root.postwalk() if n.isleaf()]
+        assert sorted(n.name for n in leaves if n.label != "loss") == genes
+    # root event probabilities from the oracle's tables
+    order = wm.order
+    arr = ccd.arrays()
+    so, sp = arr["species_offsets"], arr["species"]
+    nc = ccd.n_clades
+    spec = [set(sp[so[g]:so[g + 1]]) for g in range(nc)]
+    base, cols, o = {}, {}, 0
+    for m in order:
+        comp = [g for g in range(nc) if spec[g] <= set(m.clade)]
+        cols[m.pos] = {g: j for j, g in enumerate(comp)}
+        base[m.pos] = (o, len(comp))
+        o += (m.nslices + 1) * len(comp)
+    assert o == tab.size
+
+    def L(k, g, t):
+        c = cols[k].get(g)
+        return 0.0 if c is None else tab[base[k][0] + (t - 1) * base[k][1] + c]
+
+    root = order[-1]
+    f, h = root.children
+    top = lambda k, g: L(k, g, order[k].nslices + 1)
+    eps = om.tables([r.λ], [r.μ], q=r.q, eta=r.η, kind="ConstantDLWGD")[0]
+    offs = np.cumsum([0] + [m.nslices + 1 for m in order])
+    etop = lambda k: eps[offs[k + 1] - 1]
+    eta, er = r.η, etop(root.pos)
+    xi = 1 - (1 - eta) * er
+    cd, cs = xi * (1 - eta) / eta, eta * (1 - er) / xi ** 2
+    ub = nc - 1
+    sof, g1, g2, p = arr["split_offsets"], arr["g1"], arr["g2"], arr["p"]
+    dup = sum(p[k] * L(root.pos, g1[k], 1) * L(root.pos, g2[k], 1) * cd for k in range(sof[ub], sof[ub + 1]))
+    spe = sum(p[k] * (top(f, g1[k]) * top(h, g2[k]) + top(h, g1[k]) * top(f, g2[k])) * cs
+              for k in range(sof[ub], sof[ub + 1]))
+    los = (top(f, ub) * etop(h) + top(h, ub) * etop(f)) * cs
+    total = L(root.pos, ub, 1)
+    assert dup + spe + los == pytest.approx(total, rel=1e-10)
+    cnt = {"duplication": 0, "speciation": 0, "sploss": 0}
+    for tr in trees:
+        cnt[tr.root.label] += 1
+    for key, pr in (("duplication", dup / total), ("speciation", spe / total), ("sploss", los / total)):
+        se = np.sqrt(max(pr * (1 - pr), 1e-4) / len(trees))
+        assert abs(cnt[key] / len(trees) - pr) <= 4 * se

@@ -133,6 +133,27 @@ int wg_model_condition(const wg_model* m, double* out) {
   });
 }
 
+int wg_backtrack_tables(const wg_model* m, const wg_ccd* c, const double* tables, int64_t n_tables, int32_t n_samples,
+                        uint64_t seed, char* out, int64_t cap, int64_t* needed) {
+  WG_GUARD({
+    if (!m || !c || !tables || n_samples < 0) throw wg::Error(WG_EINVAL, "wg_backtrack_tables: bad arguments");
+    if (!m->has_params) throw wg::Error(WG_ESTATE, "model parameters not set");
+    const auto cols = wg::compat_columns(*m, *c);
+    int64_t need = 0;
+    for (int k = 0; k < m->K; ++k) {
+      int nc = 0;
+      for (int x : cols[k]) nc += x >= 0;
+      need += (int64_t)m->nrow[k] * nc;
+    }
+    if (n_tables != need) throw wg::Error(WG_EINVAL, "tables do not match the family's layout");
+    const std::string text = wg::backtrack_family(*m, *c, tables, n_samples, seed);
+    if (needed) *needed = (int64_t)text.size() + 1;
+    if (!out) return WG_OK;
+    if (cap < (int64_t)text.size() + 1) throw wg::Error(WG_ERANGE, "output buffer too small");
+    std::memcpy(out, text.c_str(), text.size() + 1);
+  });
+}
+
 int wg_ccd_parse_ale(const char* text, size_t len, const char* const* species_names, const int32_t* species_ids,
                      int32_t n_species, wg_ccd** out) {
   WG_GUARD({

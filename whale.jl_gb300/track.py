@@ -93,6 +93,23 @@ class RecTree:
     root: RecNode
 
 
+def backtrack_tables(wm: WhaleModel, ccd: CCD, tables, n: int = 1, seed: int = 0) -> List[RecTree]:
+    """Sampling from DP tables already at hand (the ``logpdf!`` layout of
+    ``Batch.family_tables``), on the host."""
+    import numpy as np
+
+    wm.load()
+    t = np.ascontiguousarray(tables, dtype=np.float64)
+    need = N.i64()
+    L = N.lib()
+    N.check(L.wg_backtrack_tables(wm._struct.h, ccd._h, N.dptr(t), t.size, int(n), C.c_uint64(seed), None, 0,
+                                  C.byref(need)))
+    buf = C.create_string_buffer(need.value)
+    N.check(L.wg_backtrack_tables(wm._struct.h, ccd._h, N.dptr(t), t.size, int(n), C.c_uint64(seed), buf,
+                                  need.value, C.byref(need)))
+    return [RecTree(ln, _parse(ln, wm)) for ln in buf.value.decode().split("\n") if ln]
+
+
 def backtrack(wm: WhaleModel, x: Union[CCD, Sequence[CCD]], n: int = 1, seed: int = 0):
     """``backtrack(wm, ccd)`` (src/track.jl:188-194): ``n`` sampled reconciled
     trees of one family (a list of RecTree); for a vector of CCDs, one such
