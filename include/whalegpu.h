@@ -137,6 +137,17 @@ int wg_batch_destroy(wg_batch* b);
 int wg_batch_info(const wg_batch* b, int32_t* n_families, int32_t* n_groups, int64_t* device_bytes,
                   double* flops_fwd, double* bytes_fwd, double* flops_adj);
 
+/* NowhereExtinctCondition (src/condition.jl:31-36, src/bdputil.jl:84-135)
+ * of model m's tree and rates, evaluated on the device (2^leaves pgf
+ * arguments, at most 22 leaves): value = log P(every leaf keeps a copy),
+ * -inf when P is not in (0, 1).  With any of d_lam, d_mu, d_q, d_eta
+ * non-null, also ∂value/∂ of the per-node natural rates λ, μ (K each), the
+ * WGD retention rates q (K, zero at other nodes) and η.  Synchronous on the
+ * context stream.  A batch whose model carries this condition evaluates it
+ * the same way, beside the DP. */
+int wg_nowhere_condition(wg_ctx* ctx, const wg_model* m, double* value, double* d_lam, double* d_mu, double* d_q,
+                         double* d_eta);
+
 /* Kernel launches in one evaluation of the batch as last recorded: forward
  * only, and forward + adjoint + gradient reduction (0 before the first call
  * of that kind).  Not in the reference (a measurement aid). */

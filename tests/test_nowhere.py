@@ -84,3 +84,28 @@ def test_host_value_and_gradient_against_oracle(W, O):
     wm = W.WhaleModel(W.DLWGD(λ=lam, μ=mu, q=q, η=0.7), t, 0.05, condition=W.NowhereExtinctCondition(t))
     om = O.OracleModel(W.nwstr(t), 0.05, condition="nowhere")
     assert W.condition(wm) == pytest.approx(om.condition(lam, mu, q=q, eta=0.7), rel=1e-12)
+
+
+def test_even_leaf_count_gives_minus_inf(W, O):
+    # treepgf_allbinary_sign (src/bdputil.jl:123-132) gives x = 1 the sign -1,
+    # i.e. (-1)^(#ones); inclusion-exclusion over the leaves left empty needs
+    # (-1)^(#zeros).  The two agree for an odd number of leaves; for an even
+    # number the reference's condition evaluates 2 - P, outside (0, 1), and
+    # returns -Inf.  The oracle and the library keep that behaviour.
+    for n_leaves in (4, 6):
+        nwk = "A:1"
+        for c in "BCDEF"[: n_leaves - 1]:
+            nwk = f"({nwk},{c}:1):0.5"
+        t = W.readnw(nwk[:-4] + ";")
+        n = len(W.postwalk(t))
+        om = O.OracleModel(W.nwstr(t), 0.1, condition="nowhere")
+        lam, mu = np.full(n, 0.05), np.full(n, 0.04)
+        assert om.condition(lam, mu, eta=0.7) == -np.inf
+        wm = W.WhaleModel(W.DLWGD(λ=np.log(lam), μ=np.log(mu), q=[], η=0.7), t, 0.1,
+                          condition=W.NowhereExtinctCondition(t))
+        assert W.condition(wm) == -np.inf
+    # with an odd number it is a probability: the 3-leaf case by hand
+    t = W.readnw("((A:1,B:1):0.5,C:1);")
+    om = O.OracleModel(W.nwstr(t), 0.1, condition="nowhere")
+    c = om.condition(np.full(5, 0.05), np.full(5, 0.04), eta=0.7)
+    assert np.isfinite(c) and c < 0.0

@@ -14,7 +14,7 @@ Tree helpers follow NewickTree: ``readnw``, ``insertnode`` (``insertnode!``),
 from ._native import WhaleError
 from .ccd import CCD, parse_ale_text, read_ale
 from .core import (Batch, Context, default_context, get_batch, gradient, logpdf, logpdf_gradient, logpdf_inplace,
-                   logpdf_plain, loglikelihood, map_gradient)
+                   logpdf_plain, loglikelihood, map_gradient, nowhere_condition)
 from .mixture import MixtureModel, ModelArray
 from .track import RecNode, RecTree, backtrack
 from .model import (ConstantDLWGD, DLWGD, NoCondition, NonExtinctCondition, NowhereExtinctCondition, RootCondition,
@@ -26,7 +26,7 @@ logpdf_ = logpdf_inplace
 
 __all__ = [
     "WhaleModel", "DLWGD", "ConstantDLWGD", "RootCondition", "NonExtinctCondition", "NoCondition",
-    "NowhereExtinctCondition", "condition",
+    "NowhereExtinctCondition", "condition", "nowhere_condition",
     "CCD", "read_ale", "parse_ale_text", "logpdf", "logpdf_inplace", "logpdf_", "loglikelihood", "gradient",
     "logpdf_gradient", "logpdf_plain", "map_gradient", "Batch", "Context", "default_context", "get_batch",
     "readnw", "nwstr", "insertnode", "getlca", "getleaves", "getroot", "postwalk", "prewalk", "extree", "EXTREE",

@@ -70,6 +70,7 @@ def _declare(L):
         "wg_pack_tasks": (C.c_int, [vp, P_vp, i32, u32, P_i32, i64, P_i64]),
         "wg_batch_info": (C.c_int, [vp, P_i32, P_i32, P_i64, P_dbl, P_dbl, P_dbl]),
         "wg_batch_launches": (C.c_int, [vp, P_i32, P_i32]),
+        "wg_nowhere_condition": (C.c_int, [vp, vp, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl]),
         "wg_backtrack": (C.c_int, [vp, vp, vp, C.c_int32, C.c_int32, C.c_uint64, C.c_char_p, C.c_int64, P_i64]),
         "wg_backtrack_tables": (C.c_int, [vp, vp, P_dbl, C.c_int64, C.c_int32, C.c_uint64, C.c_char_p, C.c_int64,
                                           P_i64]),

@@ -18,7 +18,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libwhalegpu.so")
 
 CXX_SRCS = ["wg_api.cpp", "wg_model.cpp", "wg_ccd.cpp", "wg_pack.cpp", "wg_synth.cpp", "wg_track.cpp"]
-CU_SRCS = ["wg_kernels.cu"]
+CU_SRCS = ["wg_kernels.cu", "wg_nowhere.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -42,7 +42,8 @@ def _stale(target: str, deps) -> bool:
 
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
-    headers = [os.path.join(CSRC, "wg_internal.h"), os.path.join(HERE, "..", "include", "whalegpu.h")]
+    headers = [os.path.join(CSRC, "wg_internal.h"), os.path.join(CSRC, "wg_nowhere.h"),
+               os.path.join(HERE, "..", "include", "whalegpu.h")]
     nvcc = _nvcc()
     inc = ["-I", os.path.join(_cuda_home(), "include")]
     jobs = []
@@ -52,7 +53,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
         obj = os.path.join(OUT, s + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", *inc, "-c", src, "-o", obj]
+            # no FMA contraction: host arithmetic rounds the same on x86 and Arm
+            cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", *inc,
+                   "-c", src, "-o", obj]
             jobs.append(cmd)
     for s in CU_SRCS:
         src = os.path.join(CSRC, s)

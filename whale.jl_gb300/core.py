@@ -60,6 +60,26 @@ def default_context() -> Context:
         return _default_ctx
 
 
+def nowhere_condition(wm: WhaleModel, grad: bool = False, ctx: Context = None):
+    """NowhereExtinctCondition of ``wm``'s tree and rates, on the device
+    (src/condition.jl:31-36, src/bdputil.jl:84-135): log P(every leaf keeps
+    a copy).  With ``grad``, also its derivatives on the per-node natural
+    rates λ, μ, q (positions of ``wm.order``) and on η, as a dict.  Batched
+    evaluations of a model carrying this condition compute it the same way."""
+    wm.load()
+    ctx = ctx or default_context()
+    v = N.dbl()
+    L = N.lib()
+    if not grad:
+        N.check(L.wg_nowhere_condition(ctx.h, wm._struct.h, N.C.byref(v), None, None, None, None))
+        return v.value
+    K = len(wm.order)
+    dl, dm, dq, de = np.zeros(K), np.zeros(K), np.zeros(K), np.zeros(1)
+    N.check(L.wg_nowhere_condition(ctx.h, wm._struct.h, N.C.byref(v), N.dptr(dl), N.dptr(dm), N.dptr(dq),
+                                   N.dptr(de)))
+    return v.value, {"λ": dl, "μ": dm, "q": dq, "η": float(de[0])}
+
+
 class Batch:
     """Device-resident packed families (wg_batch) for one model structure."""
 

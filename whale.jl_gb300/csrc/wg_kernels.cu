@@ -23,6 +23,7 @@
 #include <string>
 
 #include "wg_internal.h"
+#include "wg_nowhere.h"
 
 using namespace wg;
 
@@ -1166,6 +1167,7 @@ struct wg_ctx {
   bool timed_grad = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   float last_ms[3] = {0, 0, 0};
+  std::unique_ptr<NwPlan> nw;  // wg_nowhere_condition's plan
 };
 
 namespace {
@@ -1292,13 +1294,24 @@ struct wg_batch {
   double* h_famw = nullptr;
   bool weighted_pending = false;
   double cond_scale = 0.0;  // of the pending weighted evaluation
-  // captured launch sequences: [with gradient][with tables][weighted]
-  cudaGraphExec_t graph[2][2][2] = {};
-  ~wg_batch() {
+  // NowhereExtinctCondition on the device, forked beside the DP
+  std::unique_ptr<NwPlan> nw;
+  bool nw_pending = false;
+  // captured launch sequences: [with gradient][with tables][weighted][nowhere]
+  cudaGraphExec_t graph[2][2][2][2] = {};
+  void drop_graphs(int nowhere) {
     for (auto& g3 : graph)
       for (auto& g2 : g3)
-        for (auto& g : g2)
-          if (g) cudaGraphExecDestroy(g);
+        for (auto& g1 : g2)
+          if (g1[nowhere]) {
+            cudaGraphExecDestroy(g1[nowhere]);
+            g1[nowhere] = nullptr;
+          }
+  }
+  ~wg_batch() {
+    drop_graphs(0);
+    drop_graphs(1);
+    nw.reset();
     if (ctx) free_all(ctx->device, {d_famw}, {h_famw});
     plain.reset();
     subs.clear();
@@ -1606,13 +1619,23 @@ void stage_params(wg_batch* b, const wg_model* m) {
 
 // Every class's forward levels (and the reverse levels of the adjoint plus
 // its gradient reduction), forked from and joined back to the context stream.
-void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted) {
+void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted, bool nowhere) {
   wg_ctx* ctx = b->ctx;
   cudaStream_t s = ctx->stream;
   int& nl = b->launches[grad ? 1 : 0];
   nl = 0;
   ck(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(double) * (b->P + 2), cudaMemcpyHostToDevice, s),
      "params upload");
+  if (nowhere) {  // the condition depends on the rates only: beside the DP
+    NwPlan& p = *b->nw;
+    ck(cudaEventRecord(p.fork, s), "event");
+    ck(cudaStreamWaitEvent(p.s, p.fork, 0), "wait");
+    nl += nw_record(p, p.s, grad);
+    ck(cudaEventRecord(p.done, p.s), "event");
+  }
+  auto join_nw = [&] {
+    if (nowhere) ck(cudaStreamWaitEvent(s, b->nw->done, 0), "wait");
+  };
   if (weighted)
     ck(cudaMemcpyAsync(b->d_famw, b->h_famw, sizeof(double) * b->NF, cudaMemcpyHostToDevice, s), "weights upload");
   if (grad)
@@ -1666,6 +1689,7 @@ void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted) {
   }
   ck(cudaGetLastError(), "forward launch");
   join_subs(b);
+  if (!grad) join_nw();
   ck(cudaEventRecordWithFlags(ctx->ev[1], s, cudaEventRecordExternal), "event");
   if (grad) {
     fork_subs(b);
@@ -1710,6 +1734,7 @@ void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted) {
     }
     ck(cudaGetLastError(), "adjoint launch");
     join_subs(b);
+    join_nw();
     ck(cudaEventRecordWithFlags(ctx->ev[2], s, cudaEventRecordExternal), "event");
     ck(cudaEventRecordWithFlags(ctx->ev[3], s, cudaEventRecordExternal), "event");
   }
@@ -1738,13 +1763,23 @@ void enqueue(wg_batch* b, const wg_model* m, bool grad, const double* weights = 
   }
   b->weighted_pending = weighted;
   b->cond_scale = weighted ? cond_scale : (double)b->NF;
+  const bool nowhere = m->cond == WG_COND_NOWHERE;
+  if (nowhere) {
+    if (!b->nw || !nw_plan_matches(*b->nw, *m)) {
+      b->drop_graphs(1);
+      b->nw.reset();
+      b->nw = nw_plan_create(*m, ctx->device);
+    }
+    nw_stage(*b->nw, *m);
+  }
+  b->nw_pending = nowhere;
   const bool tables = grad || (b->flags & WG_BATCH_TABLES);
-  cudaGraphExec_t& ge = b->graph[grad][tables][weighted];
+  cudaGraphExec_t& ge = b->graph[grad][tables][weighted][nowhere];
   cudaStream_t s = ctx->stream;
   if (!ge) {
     ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
     try {
-      record_sequence(b, grad, tables, weighted);
+      record_sequence(b, grad, tables, weighted, nowhere);
     } catch (...) {
       cudaGraph_t g = nullptr;
       cudaStreamEndCapture(s, &g);
@@ -1782,10 +1817,11 @@ void finish_timing(wg_ctx* ctx) {
 // (src/core.jl:15, :58-64).
 void finish(const wg_model* m, int NF, const double* logl, const double* gred, bool grad, double* per_family,
             double* total, double* d_lam, double* d_mu, double* d_q, double* d_eta, double* d_eps, double* d_phi,
-            double* d_psi, const double* weights = nullptr, double cond_scale = -1.0) {
+            double* d_psi, const double* weights = nullptr, double cond_scale = -1.0,
+            const NwResult* nw = nullptr) {
   double sum = 0.0;
   for (int i = 0; i < NF; ++i) sum += weights ? (weights[i] != 0.0 ? weights[i] * logl[i] : 0.0) : logl[i];
-  const double cond = model_condition(*m);
+  const double cond = nw ? nw->value : model_condition(*m);
   const double cs = cond_scale < 0 ? (double)NF : cond_scale;
   double tot = sum - cs * cond;
   if (!std::isfinite(tot)) tot = -INFINITY;
@@ -1804,7 +1840,21 @@ void finish(const wg_model* m, int NF, const double* logl, const double* gred, b
     std::vector<double> dl, dm, dpp;
     if (d_lam || d_mu || d_q) model_tables_vjp(*m, de, dp, ds, dl, dm, dq, dpp);
     // a condition on the rates themselves (NowhereExtinct) adds its own adjoints
-    model_condition_rates_vjp(*m, -cs, dl, dm, dq, deta);
+    if (nw) {
+      if (nw->ok) {
+        dl.resize(K, 0.0);
+        dm.resize(K, 0.0);
+        dq.resize(K, 0.0);
+        for (int k = 0; k < K; ++k) {
+          dl[k] -= cs * nw->d_lam[k];
+          dm[k] -= cs * nw->d_mu[k];
+          dq[k] -= cs * nw->d_q[k];
+        }
+        deta -= cs * nw->d_eta;
+      }
+    } else {
+      model_condition_rates_vjp(*m, -cs, dl, dm, dq, deta);
+    }
     if (d_lam) std::memcpy(d_lam, dl.data(), K * sizeof(double));
     if (d_mu) std::memcpy(d_mu, dm.data(), K * sizeof(double));
   }
@@ -1830,8 +1880,14 @@ void fetch(wg_batch* b, const wg_model* m, double* per_family, double* total, do
     for (size_t i = 1; i < b->subs.size(); ++i)
       for (int j = 0; j < b->P; ++j) gred[j] += b->h_gred[i * b->P + j];
   }
+  NwResult nw;
+  if (b->nw_pending) {
+    if (m->cond != WG_COND_NOWHERE || !nw_plan_matches(*b->nw, *m))
+      throw Error(WG_ESTATE, "the model's condition changed since the evaluation was enqueued");
+    nw = nw_result(*b->nw, *m, grad);
+  }
   finish(m, b->NF, b->h_logl, gred.data(), grad, per_family, total, d_lam, d_mu, d_q, d_eta, d_eps, d_phi, d_psi,
-         b->weighted_pending ? b->h_famw : nullptr, b->cond_scale);
+         b->weighted_pending ? b->h_famw : nullptr, b->cond_scale, b->nw_pending ? &nw : nullptr);
 }
 
 void fetch_plain(PlainBatch* b, const wg_model* m, double* per_family, double* total) {
@@ -1964,6 +2020,32 @@ int wg_batch_info(const wg_batch* b, int32_t* n_families, int32_t* n_groups, int
     if (flops_fwd) *flops_fwd = b->flops_fwd;
     if (bytes_fwd) *bytes_fwd = b->bytes_fwd;
     if (flops_adj) *flops_adj = b->flops_adj;
+  });
+}
+
+int wg_nowhere_condition(wg_ctx* ctx, const wg_model* m, double* value, double* d_lam, double* d_mu, double* d_q,
+                         double* d_eta) {
+  WG_GUARD({
+    if (!ctx || !m || !value) throw Error(WG_EINVAL, "wg_nowhere_condition: bad arguments");
+    if (!m->has_params) throw Error(WG_ESTATE, "model parameters not set");
+    ck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (!ctx->nw || !nw_plan_matches(*ctx->nw, *m)) {
+      ctx->nw.reset();
+      ctx->nw = nw_plan_create(*m, ctx->device);
+    }
+    NwPlan& p = *ctx->nw;
+    const bool grad = d_lam || d_mu || d_q || d_eta;
+    nw_stage(p, *m);
+    nw_record(p, ctx->stream, grad);
+    ck(cudaStreamSynchronize(ctx->stream), "condition");
+    const NwResult r = nw_result(p, *m, grad);
+    *value = r.value;
+    for (int k = 0; grad && k < m->K; ++k) {
+      if (d_lam) d_lam[k] = r.ok ? r.d_lam[k] : 0.0;
+      if (d_mu) d_mu[k] = r.ok ? r.d_mu[k] : 0.0;
+      if (d_q) d_q[k] = r.ok ? r.d_q[k] : 0.0;
+    }
+    if (d_eta) *d_eta = r.ok ? r.d_eta : 0.0;
   });
 }
 
