@@ -16,6 +16,7 @@
  *                     getα, _ϵ, _ϕ, _ψ                                 src/bdputil.jl:6-11
  *   wg_model_condition condition(wm) (Root / NonExtinct / No)          src/condition.jl:11-29
  *   wg_ccd_*          read_ale / parse_aleobserve / CCD(ale, wm, spmap) src/ccd.jl:102-248
+ *                     (wg_ccd_read_ale_files: many files on all host threads)
  *   wg_batch_*        index_and_getℓ + per-call table allocation       src/ccd.jl:59-75, src/core.jl:41
  *   wg_logpdf         logpdf(wm, xs::Vector{CCD})                      src/core.jl:58-64
  *   wg_logpdf_grad    ForwardDiff.gradient of the above                test/runtests.jl:36-38
@@ -113,6 +114,14 @@ int wg_model_condition(const wg_model* m, double* out);
  * first '_' (src/ccd.jl:139) through species_names -> species_ids. */
 int wg_ccd_parse_ale(const char* text, size_t len, const char* const* species_names,
                      const int32_t* species_ids, int32_t n_species, wg_ccd** out);
+/* read_ale over many files (src/ccd.jl:126-137): reads and parses n_files
+ * ALE files on up to `threads` host threads (0: every core); out[i] receives
+ * the CCD of paths[i].  If any file fails, no CCD is returned, *failed (if
+ * non-null) is the index of the first failing file and the error message
+ * names it. */
+int wg_ccd_read_ale_files(const char* const* paths, int32_t n_files, const char* const* species_names,
+                          const int32_t* species_ids, int32_t n_species, int32_t threads, wg_ccd** out,
+                          int32_t* failed);
 /* Build a CCD from arrays already in the reference layout: clades ordered by
  * size with leaves first and the ubiquitous clade last; splits (g1, g2, p) with
  * 0-based clade ids and p = Dip/Bip. */

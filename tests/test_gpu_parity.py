@@ -143,3 +143,21 @@ def test_underflow_gives_minus_inf_like_reference(W, O, ex1_tree, ex1_files):
     fin = np.isfinite(oper)
     assert np.max(_rel(per[fin], oper[fin]), initial=0.0) <= REL
     assert (tot == otot) or tot == pytest.approx(otot, rel=REL)
+
+
+def test_results_do_not_depend_on_pack_threads(W, monkeypatch):
+    # the packer builds tasks on host threads and merges them in a fixed
+    # order: one thread or many give the same layout, hence bit-identical
+    # log L and gradients
+    from whale_gb300 import synth
+
+    wl = synth.config1(n_families=200)
+    wm, ccds = wl.model, wl.ccds()
+    out = []
+    for th in ("1", "0"):
+        monkeypatch.setenv("WG_PACK_THREADS", th)
+        b = W.Batch(wm, ccds, grad=True)
+        out.append(b.grad_nodes(wm))
+        del b
+    for x, y in zip(*out):
+        assert np.array_equal(np.asarray(x), np.asarray(y))

@@ -188,3 +188,56 @@ def test_truncated_ale_is_rejected(W, ex1_files):
     # a gene of a species that is not in the tree
     with pytest.raises(W.WhaleError):
         W.parse_ale_text(text.replace("ATHA_", "XXXX_"), wm)
+
+
+def test_native_multi_file_reader(W, tmp_path):
+    # wg_ccd_read_ale_files: the same CCDs as parsing each text, on 1 or many
+    # threads; a bad file fails the whole call and is named by its index
+    from whale_gb300 import synth
+
+    w = synth.config0(seed=21, n_families=24)
+    wm = w.model
+    for i, a in enumerate(w.ale):
+        (tmp_path / f"f{i:03d}.ale").write_text(a)
+    ref = [W.parse_ale_text(a, wm).arrays() for a in w.ale]
+    for th in (1, 4, 0):
+        got = W.read_ale(str(tmp_path), wm, threads=th)
+        assert [c.fname for c in got] == [f"f{i:03d}.ale" for i in range(24)]
+        for c, r in zip(got, ref):
+            a = c.arrays()
+            assert a.keys() == r.keys() and all(np.array_equal(a[k], r[k]) for k in a)
+    (tmp_path / "f010.ale").write_text(w.ale[10][: len(w.ale[10]) // 3])
+    with pytest.raises(W.WhaleError, match="f010.ale"):
+        W.read_ale(str(tmp_path), wm, threads=4)
+    from whale_gb300 import _native as N
+    from whale_gb300.ccd import _spmap_arrays
+
+    files = [str(tmp_path / f"f{i:03d}.ale") for i in range(24)]
+    enc, ids = _spmap_arrays(wm)
+    paths = (ctypes.c_char_p * 24)(*[f.encode() for f in files])
+    out = (ctypes.c_void_p * 24)()
+    failed = ctypes.c_int32(-1)
+    rc = N.lib().wg_ccd_read_ale_files(paths, 24, enc, N.iptr(ids), len(ids), 3, out, ctypes.byref(failed))
+    assert rc == -2 and failed.value == 10 and not any(out)
+
+
+def test_packing_does_not_depend_on_host_threads(W, monkeypatch):
+    from whale_gb300 import synth
+    from whale_gb300 import _native as N
+
+    w = synth.config1(n_families=150)
+    wm, ccds = w.model, w.ccds()
+    arr = (ctypes.c_void_p * len(ccds))(*[c._h for c in ccds])
+
+    def summary():
+        n = N.i64()
+        N.check(N.lib().wg_pack_tasks(wm._struct.h, arr, len(ccds), 1, None, 0, ctypes.byref(n)))
+        out = np.zeros(12 * n.value, np.int32)
+        N.check(N.lib().wg_pack_tasks(wm._struct.h, arr, len(ccds), 1, out.ctypes.data_as(N.P_i32), out.size,
+                                      ctypes.byref(n)))
+        return out
+
+    monkeypatch.setenv("WG_PACK_THREADS", "1")
+    one = summary()
+    monkeypatch.setenv("WG_PACK_THREADS", "5")
+    assert np.array_equal(one, summary())

@@ -60,6 +60,8 @@ def _declare(L):
         "wg_model_get_tables": (C.c_int, [vp, P_dbl, P_dbl, P_dbl]),
         "wg_model_condition": (C.c_int, [vp, P_dbl]),
         "wg_ccd_parse_ale": (C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(C.c_char_p), P_i32, i32, P_vp]),
+        "wg_ccd_read_ale_files": (C.c_int, [C.POINTER(C.c_char_p), i32, C.POINTER(C.c_char_p), P_i32, i32, i32, P_vp,
+                                            P_i32]),
         "wg_ccd_create": (C.c_int, [i32, P_i32, P_i32, P_i32, P_i32, P_i32, P_i32, P_dbl, i64, P_vp]),
         "wg_ccd_destroy": (C.c_int, [vp]),
         "wg_ccd_info": (C.c_int, [vp, P_i32, P_i32, P_i64, P_i32]),

@@ -9,7 +9,6 @@ addleafclades!, addubiquitous! and CCD(ale, wm, spmap) (src/ccd.jl:102-248).
 from __future__ import annotations
 
 import os
-from concurrent.futures import ThreadPoolExecutor
 from typing import List, Optional, Sequence
 
 import numpy as np
@@ -84,8 +83,10 @@ def parse_ale_text(text: str, wm, fname: str = "") -> CCD:
     return CCD(h, fname)
 
 
-def read_ale(path: str, wm, threads: int = 8) -> List[CCD]:
-    """``read_ale(s, wm)`` (src/ccd.jl:126-137)."""
+def read_ale(path: str, wm, threads: int = 0) -> List[CCD]:
+    """``read_ale(s, wm)`` (src/ccd.jl:126-137): one file, a directory (its
+    files in sorted order) or a file listing paths.  The files are read and
+    parsed natively on ``threads`` host threads (0: every core)."""
     if not os.path.exists(path):
         raise FileNotFoundError(f"Not a file nor directory `{path}`")
     if os.path.isfile(path) and path.endswith(".ale"):
@@ -98,15 +99,10 @@ def read_ale(path: str, wm, threads: int = 8) -> List[CCD]:
             files = [os.path.join(path, f) for f in sorted(os.listdir(path))]
         files = [f for f in files if not f.startswith("#")]
     enc, ids = _spmap_arrays(wm)
-
-    def one(f):
-        with open(f, "rb") as fh:
-            b = fh.read()
-        h = N.vp()
-        N.check(N.lib().wg_ccd_parse_ale(b, len(b), enc, N.iptr(ids), len(ids), N.C.byref(h)))
-        return CCD(h, os.path.basename(f))
-
-    if len(files) == 1 or threads <= 1:
-        return [one(f) for f in files]
-    with ThreadPoolExecutor(max_workers=threads) as ex:
-        return list(ex.map(one, files))
+    n = len(files)
+    paths = (N.C.c_char_p * max(n, 1))(*[f.encode() for f in files])
+    out = (N.vp * max(n, 1))()
+    failed = N.C.c_int32(-1)
+    N.check(N.lib().wg_ccd_read_ale_files(paths, n, enc, N.iptr(ids), len(ids), int(threads), out,
+                                          N.C.byref(failed)))
+    return [CCD(N.vp(out[i]), os.path.basename(f)) for i, f in enumerate(files)]

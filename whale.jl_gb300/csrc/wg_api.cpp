@@ -3,7 +3,10 @@
 // wg_kernels.cu.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <string>
 
 #include "wg_internal.h"
@@ -167,6 +170,56 @@ int wg_ccd_parse_ale(const char* text, size_t len, const char* const* species_na
     static_cast<wg::CCD&>(*h) = std::move(*c);
     delete c;
     *out = h;
+  });
+}
+
+int wg_ccd_read_ale_files(const char* const* paths, int32_t n_files, const char* const* species_names,
+                          const int32_t* species_ids, int32_t n_species, int32_t threads, wg_ccd** out,
+                          int32_t* failed) {
+  WG_GUARD({
+    if (!paths || n_files < 0 || !out || (n_species > 0 && (!species_names || !species_ids)))
+      throw wg::Error(WG_EINVAL, "wg_ccd_read_ale_files: bad arguments");
+    if (failed) *failed = -1;
+    std::vector<std::string> names;
+    std::vector<int> ids;
+    for (int i = 0; i < n_species; ++i) { names.emplace_back(species_names[i]); ids.push_back(species_ids[i]); }
+    std::vector<wg_ccd*> res((size_t)n_files, nullptr);
+    std::mutex mu;
+    int64_t bad = n_files;
+    int code = WG_OK;
+    std::string msg;
+    wg::parallel_for((size_t)n_files, threads, [&](size_t i) {
+      try {
+        std::string text;
+        {
+          FILE* f = paths[i] ? std::fopen(paths[i], "rb") : nullptr;
+          if (!f) throw wg::Error(WG_EINVAL, "cannot open file");
+          char buf[1 << 16];
+          for (size_t r; (r = std::fread(buf, 1, sizeof buf, f)) > 0;) text.append(buf, r);
+          const bool err = std::ferror(f) != 0;
+          std::fclose(f);
+          if (err) throw wg::Error(WG_EINVAL, "read error");
+        }
+        std::unique_ptr<wg::CCD> c(wg::parse_ale(text.data(), text.size(), names, ids));
+        auto* h = new wg_ccd();
+        static_cast<wg::CCD&>(*h) = std::move(*c);
+        res[i] = h;
+      } catch (const std::exception& e) {
+        const wg::Error* we = dynamic_cast<const wg::Error*>(&e);
+        std::lock_guard<std::mutex> lk(mu);
+        if ((int64_t)i < bad) {
+          bad = (int64_t)i;
+          code = we ? we->code : WG_EINVAL;
+          msg = std::string(paths[i] ? paths[i] : "(null)") + ": " + e.what();
+        }
+      }
+    });
+    if (bad < n_files) {
+      for (wg_ccd* h : res) delete h;
+      if (failed) *failed = (int32_t)bad;
+      throw wg::Error(code, msg);
+    }
+    std::copy(res.begin(), res.end(), out);
   });
 }
 

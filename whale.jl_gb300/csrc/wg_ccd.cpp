@@ -19,6 +19,7 @@
 #include <cstring>
 #include <string>
 #include <map>
+#include <memory>
 #include <unordered_map>
 
 #include "wg_internal.h"
@@ -34,18 +35,6 @@ struct Cursor {
 
 inline bool is_space(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\n'; }
 
-// Split a section body into whitespace-separated tokens per line.
-void tokens_of_line(const char* b, const char* e, std::vector<std::pair<const char*, size_t>>& out) {
-  out.clear();
-  const char* p = b;
-  while (p < e) {
-    while (p < e && is_space(*p)) ++p;
-    const char* s = p;
-    while (p < e && !is_space(*p)) ++p;
-    if (p > s) out.emplace_back(s, (size_t)(p - s));
-  }
-}
-
 int64_t to_i64(const std::pair<const char*, size_t>& t) {
   int64_t v = 0;
   bool neg = false;
@@ -60,13 +49,74 @@ int64_t to_i64(const std::pair<const char*, size_t>& t) {
   return neg ? -v : v;
 }
 
-struct Hash64 {
-  size_t operator()(const std::vector<uint64_t>& v) const {
-    uint64_t h = 1469598103934665603ull;
-    for (uint64_t x : v) { h ^= x + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2); }
-    return (size_t)h;
+
+// Tokens of one line [b, e) as integers or spans.  The reference deletes
+// every ":\t" from a line before splitting it (src/ccd.jl:154); where each
+// ':' is followed by a tab and preceded by whitespace (or starts the line),
+// as in the set-id lines "12\t:\t3\t4", that equals reading ":\t" as blanks,
+// which the scanner does in place.  Other lines take the literal deletion.
+struct LineTokens {
+  std::vector<std::pair<const char*, size_t>> tok;
+  std::string buf;
+  void split(const char* b, const char* e) {
+    bool fast = true;  // every ':' reads as a blank
+    for (const char* c = (const char*)memchr(b, ':', (size_t)(e - b)); c;
+         c = c + 1 < e ? (const char*)memchr(c + 1, ':', (size_t)(e - c - 1)) : nullptr)
+      if (c + 1 >= e || c[1] != '\t' || (c > b && !is_space(c[-1]))) {
+        fast = false;
+        break;
+      }
+    if (!fast) {
+      buf.assign(b, e);
+      for (size_t pos = buf.find(":\t"); pos != std::string::npos; pos = buf.find(":\t", pos)) buf.erase(pos, 2);
+      b = buf.data();
+      e = b + buf.size();
+    }
+    tok.clear();
+    auto blank = [&](char ch) { return is_space(ch) || (fast && ch == ':'); };
+    const char* p = b;
+    while (p < e) {
+      while (p < e && blank(*p)) ++p;
+      const char* st = p;
+      while (p < e && !blank(*p)) ++p;
+      if (p > st) tok.emplace_back(st, (size_t)(p - st));
+    }
   }
 };
+
+// A line of integers separated by blanks (and ":\t" read as a blank under
+// the same rule as LineTokens) straight into `out`; false when the line has
+// anything else, for the general path to handle (and report).
+bool scan_ints(const char* b, const char* e, std::vector<int64_t>& out) {
+  out.clear();
+  const char* p = b;
+  while (p < e) {
+    const char ch = *p;
+    if (is_space(ch)) {
+      ++p;
+      continue;
+    }
+    if (ch == ':') {
+      if (p + 1 >= e || p[1] != '\t' || (p > b && !is_space(p[-1]))) return false;
+      p += 2;
+      continue;
+    }
+    bool neg = false;
+    if (ch == '-' || ch == '+') neg = ch == '-', ++p;
+    if (p >= e || *p < '0' || *p > '9') return false;
+    int64_t v = 0;
+    while (p < e && *p >= '0' && *p <= '9') v = v * 10 + (*p++ - '0');
+    if (p < e && !is_space(*p) && *p != ':') return false;
+    out.push_back(neg ? -v : v);
+  }
+  return true;
+}
+
+int64_t count_lines(const char* b, const char* e) {
+  int64_t n = 0;
+  for (const char* p = b; p < e; ++p) n += *p == '\n';
+  return n + 1;
+}
 
 }  // namespace
 
@@ -85,12 +135,9 @@ CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& nam
     }
   }
   if (parts.size() < 2 || parts.size() - 2 != 8) throw Error(WG_EPARSE, "Not a valid .ale file (expected 8 sections)");
-  int64_t observations = -1;
-  std::unordered_map<int64_t, int64_t> bip;
-  std::unordered_map<int64_t, std::vector<std::array<int64_t, 3>>> dip;
-  std::map<int64_t, std::vector<int64_t>> set_id;     // ordered by key (sort!(OrderedDict(...)))
-  std::unordered_map<int64_t, std::string> leaf_id;  // leaf number -> gene name
-  std::vector<std::pair<const char*, size_t>> tok;
+  enum Kind { OTHER, OBS, BIP, DIP, SETID, LEAFID };
+  struct Sec { Kind kind; const char* b; const char* e; };
+  std::vector<Sec> secs;
   for (size_t si = 1; si + 1 < parts.size(); ++si) {
     const char* b = parts[si].first;
     const char* e = parts[si].second;
@@ -98,104 +145,169 @@ CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& nam
     std::string header(b, nl ? nl : e);
     while (!header.empty() && (header.back() == '\r' || header.back() == ' ')) header.pop_back();
     for (char& c : header) if (c == '-') c = '_';
-    const char* p = nl ? nl + 1 : e;
+    const Kind k = header == "observations" ? OBS : header == "Bip_counts" ? BIP : header == "Dip_counts" ? DIP
+                 : header == "set_id" ? SETID : header == "leaf_id" ? LEAFID : OTHER;
+    secs.push_back({k, nl ? nl + 1 : e, e});
+  }
+  // Set ids must end up contiguous 1..G-1 (checked below), so every table
+  // keyed by a set id is a vector over 0..G; keys outside are never read.
+  int64_t set_lines = 0, leaf_lines = 0;  // leaf_lines: largest leaf number
+  LineTokens lt;
+  auto& tok = lt.tok;
+  std::vector<std::pair<int64_t, std::string>> leaves;
+  for (auto& sc : secs) {
+    if (sc.kind == SETID) set_lines += count_lines(sc.b, sc.e);
+    if (sc.kind != LEAFID) continue;
+    for (const char* p = sc.b; p < sc.e;) {
+      const char* le = (const char*)memchr(p, '\n', (size_t)(sc.e - p));
+      if (!le) le = sc.e;
+      lt.split(p, le);
+      p = le + (le < sc.e ? 1 : 0);
+      if (tok.empty()) continue;
+      if (tok.size() < 2) throw Error(WG_EPARSE, "ALE: bad leaf-id line");
+      const int64_t id = to_i64(tok[1]);
+      if (id < 0 || id > (int64_t)1 << 31) throw Error(WG_EPARSE, "ALE: leaf id out of range");
+      leaves.emplace_back(id, std::string(tok[0].first, tok[0].second));
+      leaf_lines = std::max(leaf_lines, id);
+    }
+  }
+  const int64_t cap = set_lines + 2;  // ids 0..set_lines, plus the ubiquitous clade
+  int64_t observations = -1;
+  std::vector<int64_t> bip(cap + 1, 0);
+  std::vector<char> has_bip(cap + 1, 0), has_dip(cap + 1, 0), has_set(cap + 1, 0);
+  std::vector<std::vector<std::array<int64_t, 3>>> dip(cap + 1);
+  std::vector<std::vector<int64_t>> set_id(cap + 1);
+  std::vector<std::string> leaf_id(leaf_lines + 1);  // leaf number -> gene name
+  std::vector<char> has_leaf(leaf_lines + 1, 0);
+  for (auto& l : leaves) leaf_id[l.first] = std::move(l.second), has_leaf[l.first] = 1;
+  std::vector<int64_t> ints;
+  for (auto& sc : secs) {
+    if (sc.kind == OTHER || sc.kind == LEAFID) continue;
+    const char* p = sc.b;
+    const char* e = sc.e;
+    std::vector<int64_t>& v = ints;
     while (p < e) {
       const char* le = (const char*)memchr(p, '\n', (size_t)(e - p));
       if (!le) le = e;
-      // remove ":\t" (src/ccd.jl:154): it only occurs as the set-id separator
-      std::string line(p, le);
-      for (size_t pos = line.find(":\t"); pos != std::string::npos; pos = line.find(":\t", pos)) line.erase(pos, 2);
-      tokens_of_line(line.data(), line.data() + line.size(), tok);
+      if (!scan_ints(p, le, v)) {  // not all integers: the general path converts (and reports)
+        lt.split(p, le);
+        v.clear();
+        for (auto& t : tok) v.push_back(to_i64(t));
+      }
       p = le + (le < e ? 1 : 0);
-      if (tok.empty()) continue;
-      if (header == "observations") {
-        observations = to_i64(tok[0]);
-      } else if (header == "Bip_counts") {
-        if (tok.size() < 2) throw Error(WG_EPARSE, "ALE: bad Bip_counts line");
-        bip[to_i64(tok[0])] = to_i64(tok[1]);
-      } else if (header == "Dip_counts") {
-        if (tok.size() < 4) throw Error(WG_EPARSE, "ALE: bad Dip_counts line");
-        dip[to_i64(tok[0])].push_back({to_i64(tok[1]), to_i64(tok[2]), to_i64(tok[3])});
-      } else if (header == "set_id") {
-        std::vector<int64_t> v;
-        for (size_t k = 1; k < tok.size(); ++k) v.push_back(to_i64(tok[k]));
-        set_id[to_i64(tok[0])] = std::move(v);
-      } else if (header == "leaf_id") {
-        if (tok.size() < 2) throw Error(WG_EPARSE, "ALE: bad leaf-id line");
-        leaf_id[to_i64(tok[1])] = std::string(tok[0].first, tok[0].second);
+      if (v.empty()) continue;
+      switch (sc.kind) {
+        case OBS:
+          observations = v[0];
+          break;
+        case BIP: {
+          if (v.size() < 2) throw Error(WG_EPARSE, "ALE: bad Bip_counts line");
+          if (v[0] >= 0 && v[0] <= cap) bip[v[0]] = v[1], has_bip[v[0]] = 1;
+          break;
+        }
+        case DIP: {
+          if (v.size() < 4) throw Error(WG_EPARSE, "ALE: bad Dip_counts line");
+          if (v[0] >= 0 && v[0] <= cap) dip[v[0]].push_back({v[1], v[2], v[3]}), has_dip[v[0]] = 1;
+          break;
+        }
+        case SETID: {
+          const int64_t id = v[0];
+          if (id < 1 || id >= cap) throw Error(WG_EPARSE, "ALE: set ids are not contiguous 1..n");
+          set_id[id].assign(v.begin() + 1, v.end());
+          has_set[id] = 1;
+          break;
+        }
+        default:
+          break;
       }
     }
   }
   if (observations < 0) throw Error(WG_EPARSE, "ALE: missing observations");
   // addleafclades!
-  std::unordered_map<int64_t, std::string> leafname;  // leaf set id -> gene name
-  std::unordered_map<int64_t, int64_t> themap;        // leaf id -> set id
-  for (auto& kv : set_id) {
-    auto& v = kv.second;
+  std::vector<std::string> leafname(cap + 1);  // leaf set id -> gene name
+  std::vector<char> is_leafset(cap + 1, 0);
+  std::vector<int64_t> themap(leaf_lines + 1, -1);  // leaf id -> set id
+  for (int64_t k = 1; k < cap; ++k) {
+    if (!has_set[k]) continue;
+    auto& v = set_id[k];
     if (v.size() == 1) {
-      auto it = leaf_id.find(v[0]);
-      if (it == leaf_id.end()) throw Error(WG_EPARSE, "ALE: leaf id without a name");
-      bip[kv.first] = observations;
-      dip[kv.first].clear();
-      leafname[kv.first] = it->second;
-      themap[v[0]] = kv.first;
+      const int64_t x = v[0];
+      if (x < 0 || x > leaf_lines || !has_leaf[x]) throw Error(WG_EPARSE, "ALE: leaf id without a name");
+      bip[k] = observations, has_bip[k] = 1;
+      dip[k].clear(), has_dip[k] = 1;
+      leafname[k] = leaf_id[x];
+      is_leafset[k] = 1;
+      themap[x] = k;
     } else {
       for (auto& x : v) {
-        auto it = themap.find(x);
-        if (it == themap.end()) throw Error(WG_EPARSE, "ALE: set refers to an unknown leaf");
-        x = it->second;
+        if (x < 0 || x > leaf_lines || themap[x] < 0) throw Error(WG_EPARSE, "ALE: set refers to an unknown leaf");
+        x = themap[x];
       }
     }
   }
-  for (auto& kv : themap) set_id[kv.second] = {kv.second};
+  for (int64_t x = 0; x <= leaf_lines; ++x)
+    if (themap[x] >= 0) set_id[themap[x]] = {themap[x]};
   // addubiquitous!
-  const int64_t G = (int64_t)set_id.size() + 1;
-  const size_t n = leafname.size();
+  int64_t nset = 0, kmin = -1, kmax = -1;
+  for (int64_t k = 1; k < cap; ++k)
+    if (has_set[k]) ++nset, kmax = k, kmin = kmin < 0 ? k : kmin;
+  const int64_t G = nset + 1;
+  size_t n = 0;
+  for (int64_t k = 1; k < cap; ++k) n += is_leafset[k];
   if (n < 2) throw Error(WG_EPARSE, "ALE: fewer than two leaves");
-  if (set_id.begin()->first != 1 || set_id.rbegin()->first != G - 1)
-    throw Error(WG_EPARSE, "ALE: set ids are not contiguous 1..n");
+  if (kmin != 1 || kmax != G - 1) throw Error(WG_EPARSE, "ALE: set ids are not contiguous 1..n");
   // leaf bit index: rank of each leaf set id
-  std::unordered_map<int64_t, int> leafbit;
+  std::vector<int> leafbit(cap + 1, -1);
   {
-    std::vector<int64_t> ls;
-    for (auto& kv : leafname) ls.push_back(kv.first);
-    std::sort(ls.begin(), ls.end());
-    for (size_t i = 0; i < ls.size(); ++i) leafbit[ls[i]] = (int)i;
+    int r = 0;
+    for (int64_t k = 1; k < G; ++k)
+      if (is_leafset[k]) leafbit[k] = r++;
   }
   const int W = (int)((n + 63) / 64);
-  std::vector<std::vector<uint64_t>> bits(G);
-  std::unordered_map<std::vector<uint64_t>, int64_t, Hash64> byset;
-  for (auto& kv : set_id) {
-    std::vector<uint64_t> b(W, 0);
-    for (int64_t x : kv.second) {
-      auto it = leafbit.find(x);
-      if (it == leafbit.end()) throw Error(WG_EPARSE, "ALE: set refers to a non-leaf set");
-      b[it->second >> 6] |= 1ull << (it->second & 63);
+  std::vector<uint64_t> bits((size_t)G * W, 0);
+  auto hash_row = [W](const uint64_t* r) {
+    uint64_t h = 1469598103934665603ull;
+    for (int w = 0; w < W; ++w) h ^= r[w] + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+    return h;
+  };
+  // sets by (hash of the leaf bitset, id): the first id of equal sets wins
+  // the complement lookup, as the first insert into a map keyed by the set
+  std::vector<std::pair<uint64_t, int64_t>> byset;
+  byset.reserve((size_t)G);
+  for (int64_t k = 1; k < G; ++k) {
+    uint64_t* b = bits.data() + (size_t)k * W;
+    for (int64_t x : set_id[k]) {
+      if (x < 1 || x >= G || leafbit[x] < 0) throw Error(WG_EPARSE, "ALE: set refers to a non-leaf set");
+      b[leafbit[x] >> 6] |= 1ull << (leafbit[x] & 63);
     }
-    bits[kv.first] = b;
-    byset.emplace(b, kv.first);
+    byset.emplace_back(hash_row(b), k);
   }
+  std::sort(byset.begin(), byset.end());
+  auto find_set = [&](const uint64_t* r) -> int64_t {
+    auto it = std::lower_bound(byset.begin(), byset.end(), std::make_pair(hash_row(r), (int64_t)0));
+    for (; it != byset.end() && it->first == hash_row(r); ++it)
+      if (std::memcmp(bits.data() + (size_t)it->second * W, r, sizeof(uint64_t) * W) == 0) return it->second;
+    return -1;
+  };
   std::vector<uint64_t> all(W, 0);
   for (size_t i = 0; i < n; ++i) all[i >> 6] |= 1ull << (i & 63);
   std::vector<std::array<int64_t, 3>> rootsplits;
   int64_t N = 0;
+  std::vector<uint64_t> c(W);
   for (int64_t i = 1; i < G; ++i) {
-    std::vector<uint64_t> c(W);
     bool empty = true;
-    for (int w = 0; w < W; ++w) { c[w] = all[w] & ~bits[i][w]; empty &= c[w] == 0; }
+    for (int w = 0; w < W; ++w) { c[w] = all[w] & ~bits[(size_t)i * W + w]; empty &= c[w] == 0; }
     if (empty) continue;
-    auto it = byset.find(c);
-    if (it == byset.end() || it->second <= i) continue;
-    const int64_t j = it->second;
-    auto bi = bip.find(i), bj = bip.find(j);
-    if (bi == bip.end() || bj == bip.end()) throw Error(WG_EPARSE, "ALE: missing Bip count");
-    if (bi->second != bj->second) throw Error(WG_EPARSE, "ALE: complementary clades have different Bip counts");
-    N += bi->second;
-    rootsplits.push_back({i, j, bj->second});
+    const int64_t j = find_set(c.data());
+    if (j < 0 || j <= i) continue;
+    if (!has_bip[i] || !has_bip[j]) throw Error(WG_EPARSE, "ALE: missing Bip count");
+    if (bip[i] != bip[j]) throw Error(WG_EPARSE, "ALE: complementary clades have different Bip counts");
+    N += bip[i];
+    rootsplits.push_back({i, j, bip[j]});
   }
   if (rootsplits.empty()) throw Error(WG_EPARSE, "ALE: no complementary clade pairs for the root");
-  dip[G] = rootsplits;
-  bip[G] = N;
+  dip[G] = rootsplits, has_dip[G] = 1;
+  bip[G] = N, has_bip[G] = 1;
   {
     std::vector<int64_t> u = set_id[rootsplits.back()[0]];
     const auto& v = set_id[rootsplits.back()[1]];
@@ -205,55 +317,62 @@ CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& nam
   }
   // CCD(ale, wm, spmap): order by (size, key)
   std::vector<std::pair<size_t, int64_t>> ord;
-  ord.reserve(set_id.size());
-  for (auto& kv : set_id) ord.emplace_back(kv.second.size(), kv.first);
+  ord.reserve((size_t)G);
+  for (int64_t k = 1; k <= G; ++k) ord.emplace_back(set_id[k].size(), k);
   std::sort(ord.begin(), ord.end());
-  std::unordered_map<int64_t, int> idmap;
+  std::vector<int> idmap(cap + 1, -1);
   for (size_t i = 0; i < ord.size(); ++i) idmap[ord[i].second] = (int)i;
   std::unordered_map<std::string, int> spmap;
   for (size_t i = 0; i < names.size(); ++i) spmap[names[i]] = ids[i];
-  std::unordered_map<int64_t, int> leafsp;
-  for (auto& kv : leafname) {
-    const std::string& nm = kv.second;
+  std::vector<int> leafsp(cap + 1, -1);
+  for (int64_t k = 1; k < G; ++k) {
+    if (!is_leafset[k]) continue;
+    const std::string& nm = leafname[k];
     const std::string pre = nm.substr(0, nm.find('_'));
     auto it = spmap.find(pre);
     if (it == spmap.end()) throw Error(WG_EPARSE, "ALE: gene '" + nm + "' has no species '" + pre + "' in the tree");
-    leafsp[kv.first] = it->second;
+    leafsp[k] = it->second;
   }
-  auto* c = new CCD();
-  c->n_clades = (int)ord.size();
-  c->observations = observations;
-  c->n_genes = (int)n;
-  c->sp_off.push_back(0);
-  c->split_off.push_back(0);
+  auto* cc = new CCD();
+  std::unique_ptr<CCD> guard(cc);
+  cc->n_clades = (int)ord.size();
+  cc->observations = observations;
+  cc->n_genes = (int)n;
+  {
+    size_t nsplit = 0;
+    for (auto& o : ord) nsplit += dip[o.second].size();
+    cc->g1.reserve(nsplit), cc->g2.reserve(nsplit), cc->p.reserve(nsplit);
+    for (auto* v : {&cc->nleaves, &cc->split_off, &cc->sp_off}) v->reserve(ord.size() + 1);
+    cc->counts.reserve(ord.size());
+    cc->leaf_name.reserve(ord.size());
+    cc->sp.reserve(ord.size() * 4);
+  }
+  cc->sp_off.push_back(0);
+  cc->split_off.push_back(0);
   std::vector<int> sp;
   for (size_t i = 0; i < ord.size(); ++i) {
     const int64_t k = ord[i].second;
-    auto bi = bip.find(k);
-    if (bi == bip.end()) throw Error(WG_EPARSE, "ALE: clade without a Bip count");
-    c->nleaves.push_back((int)ord[i].first);
-    c->leaf_name.push_back(ord[i].first == 1 ? leafname.at(*set_id[k].begin()) : std::string());
-    c->counts.push_back(bi->second);
-    auto di = dip.find(k);
-    if (di == dip.end() && ord[i].first > 1) throw Error(WG_EPARSE, "ALE: clade without Dip counts");
-    if (di != dip.end()) {
-      for (auto& t : di->second) {
-        auto a = idmap.find(t[0]), b = idmap.find(t[1]);
-        if (a == idmap.end() || b == idmap.end()) throw Error(WG_EPARSE, "ALE: split refers to an unknown set");
-        c->g1.push_back(a->second);
-        c->g2.push_back(b->second);
-        c->p.push_back((double)t[2] / (double)bi->second);
-      }
+    if (!has_bip[k]) throw Error(WG_EPARSE, "ALE: clade without a Bip count");
+    cc->nleaves.push_back((int)ord[i].first);
+    cc->leaf_name.push_back(ord[i].first == 1 ? leafname[set_id[k][0]] : std::string());
+    cc->counts.push_back(bip[k]);
+    if (!has_dip[k] && ord[i].first > 1) throw Error(WG_EPARSE, "ALE: clade without Dip counts");
+    for (auto& t : dip[k]) {
+      const int a = t[0] >= 0 && t[0] <= cap ? idmap[t[0]] : -1, b = t[1] >= 0 && t[1] <= cap ? idmap[t[1]] : -1;
+      if (a < 0 || b < 0) throw Error(WG_EPARSE, "ALE: split refers to an unknown set");
+      cc->g1.push_back(a);
+      cc->g2.push_back(b);
+      cc->p.push_back((double)t[2] / (double)bip[k]);
     }
-    c->split_off.push_back((int)c->g1.size());
+    cc->split_off.push_back((int)cc->g1.size());
     sp.clear();
-    for (int64_t x : set_id[k]) sp.push_back(leafsp.at(x));
+    for (int64_t x : set_id[k]) sp.push_back(leafsp[x]);
     std::sort(sp.begin(), sp.end());
     sp.erase(std::unique(sp.begin(), sp.end()), sp.end());
-    c->sp.insert(c->sp.end(), sp.begin(), sp.end());
-    c->sp_off.push_back((int)c->sp.size());
+    cc->sp.insert(cc->sp.end(), sp.begin(), sp.end());
+    cc->sp_off.push_back((int)cc->sp.size());
   }
-  return c;
+  return guard.release();
 }
 
 }  // namespace wg

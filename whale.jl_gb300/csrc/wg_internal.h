@@ -2,9 +2,14 @@
 // of libwhalegpu.  Nothing here is part of the public ABI (include/whalegpu.h).
 #pragma once
 
+#include <algorithm>
+#include <atomic>
 #include <cstdint>
+#include <cstdlib>
+#include <exception>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/whalegpu.h"
@@ -18,6 +23,39 @@ struct Error : std::runtime_error {
 };
 
 void set_last_error(const std::string& msg);
+
+// Host threads of the packer: WG_PACK_THREADS when set, else 0 (every core).
+inline int default_host_threads() {
+  const char* e = std::getenv("WG_PACK_THREADS");
+  return e ? std::atoi(e) : 0;
+}
+
+// fn(i) for i < n on up to `threads` host threads (0: all cores); the first
+// exception is rethrown here.
+template <class F>
+void parallel_for(size_t n, int threads, F fn) {
+  unsigned nt = threads > 0 ? (unsigned)threads : std::max(1u, std::thread::hardware_concurrency());
+  nt = (unsigned)std::min<size_t>({(size_t)nt, (size_t)64, n});
+  if (nt <= 1) {
+    for (size_t i = 0; i < n; ++i) fn(i);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  std::vector<std::exception_ptr> err(nt);
+  std::vector<std::thread> pool;
+  for (unsigned t = 0; t < nt; ++t)
+    pool.emplace_back([&, t] {
+      try {
+        for (size_t i; (i = next.fetch_add(1)) < n;) fn(i);
+      } catch (...) {
+        err[t] = std::current_exception();
+        next = n;
+      }
+    });
+  for (auto& th : pool) th.join();
+  for (auto& e : err)
+    if (e) std::rethrow_exception(e);
+}
 
 // ---------------------------------------------------------------------------
 // Species-tree model: the node order, per-node slice shapes and species sets
@@ -281,6 +319,7 @@ struct PackOptions2 {
   bool keep_tables = false;
   bool adjoint = false;
   const std::vector<int>* global_ids = nullptr;  // family index written to log L outputs
+  int threads = default_host_threads();  // host threads building tasks; the layout does not depend on it
 };
 
 Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const PackOptions2& opt);

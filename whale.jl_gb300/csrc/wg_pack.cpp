@@ -21,9 +21,12 @@
 // The transposed programs the adjoint needs are built here as well.
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <numeric>
+#include <thread>
 
 #include "wg_internal.h"
 
@@ -510,6 +513,18 @@ namespace wg {
 
 namespace {
 
+// A task built apart from the others: its programs' entries, int tables,
+// staging map and level programs with task-local offsets.
+struct TaskBuild {
+  DTask T;
+  std::vector<DEntry> entries;
+  std::vector<int32_t> meta;
+  std::vector<int64_t> gmap;
+  std::vector<DProg2> progs;
+  std::vector<int> col;  // first row position of each family of the group
+  int smem_adj = 0, NT = 0;
+};
+
 struct Item {
   int c = 0;                  // output position of the finalize op
   uint32_t fin = op::FIN_DUP;
@@ -648,15 +663,19 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
   // ---- per family: compatibility, levels, cost
   std::vector<FamInfo> info(NF);
   std::vector<std::vector<int>> lvl(NF);
-  for (int f = 0; f < NF; ++f) {
+  std::vector<std::array<double, 3>> cost(NF);
+  for (int f = 0; f < NF; ++f)
     if (ccds[f]->n_clades >= 65535) throw Error(WG_ERANGE, "CCD with 65535 or more clades");
+  parallel_for(NF, opt.threads, [&](size_t f) {
     compat_of(m, *ccds[f], info[f], true);
-    double fl, by, fa, w;
-    family_cost(m, *ccds[f], info[f], fl, by, fa, w);
-    P.flops_fwd += fl;
-    P.bytes_fwd += by;
-    P.flops_adj += fa;
+    double w;
+    family_cost(m, *ccds[f], info[f], cost[f][0], cost[f][1], cost[f][2], w);
     lvl[f] = split_levels(*ccds[f]);
+  });
+  for (int f = 0; f < NF; ++f) {  // summed in family order
+    P.flops_fwd += cost[f][0];
+    P.bytes_fwd += cost[f][1];
+    P.flops_adj += cost[f][2];
   }
   // per (family, node) location of the top row, filled as tasks are built
   std::vector<int64_t> toploc((size_t)NF * K, -1);
@@ -682,6 +701,9 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
   P.level_smem_adj_h.assign(H + 1, 0);
   // gradient reduction contributions
   std::vector<std::vector<int64_t>> red(3 * (size_t)NR + K + 1);
+  std::vector<std::vector<DEntry>> entry_chunks;
+  std::vector<int64_t> entry_off;
+  int64_t n_entries = 0;
   auto eps_top_row = [&](int k) { return m.row_off[k] + m.nrow[k] - 1; };
 
   for (int k = 0; k < K; ++k) {
@@ -726,10 +748,14 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       }
       if (!cur.empty()) { groups.push_back(cur); group_ops.push_back(ops); }
     }
-    for (size_t gi = 0; gi < groups.size(); ++gi) {
+    // one task per group, built in parallel into task-local buffers and
+    // merged in group order (global offsets assigned there)
+    auto build = [&](size_t gi, TaskBuild& tb) {
       const auto& fams = groups[gi];
+      DTask& T = tb.T;
+      std::vector<DEntry>& entries = tb.entries;
+      std::vector<int32_t>& meta = tb.meta;
       const int nf = (int)fams.size();
-      DTask T;
       T.node = k;
       T.nfam = nf;
       const double gops = group_ops[gi];
@@ -754,28 +780,14 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       auto pos = [&](int i, int g) { const int j = info[fams[i]].idx[k][g]; return j < 0 ? -1 : col[i] + j; };
       auto posa = [&](int i, int g) { const int j = info[fams[i]].idx[ka][g]; return j < 0 ? -1 : cola[i] + j; };
       auto posb = [&](int i, int g) { const int j = info[fams[i]].idx[kb][g]; return j < 0 ? -1 : colb[i] + j; };
-      T.top = P.tops_doubles;
-      P.tops_doubles += R;
-      if (opt.keep_tables) {
-        T.tab = P.tab_doubles;
-        P.tab_doubles += (int64_t)m.nrow[k] * R;
-      }
-      for (int i = 0; i < nf; ++i) {
-        const size_t fk = (size_t)fams[i] * K + k;
-        toploc[fk] = T.top + col[i];
-        P.fam_tab[fk] = T.tab;
-        P.fam_w[fk] = R;
-        P.fam_col[fk] = col[i];
-        P.fam_ncol[fk] = info[fams[i]].ncompat[k];
-      }
+      tb.col = col;
       // staging maps of the children's top rows
-      T.gmap = (int64_t)P.gmap.size();
-      for (int ch : {ka, kb}) {
+      for (int ch : {ka, kb}) {  // children's tops are final: their nodes came first
         if (ch < 0) continue;
         for (int i = 0; i < nf; ++i) {
           const int C = info[fams[i]].ncompat[ch];
           const int64_t src = toploc[(size_t)fams[i] * K + ch];
-          for (int j = 0; j < C; ++j) P.gmap.push_back(src + j);
+          for (int j = 0; j < C; ++j) tb.gmap.push_back(src + j);
         }
       }
       // ---- forward programs
@@ -811,8 +823,8 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
             items.push_back(std::move(it));
           }
         }
-        if (has_rows) T.dup = schedule2(items, NT, opt.target_j, P.entries);
-        if (opt.adjoint) T.tdup = schedule2(titems, NT, opt.target_j, P.entries);
+        if (has_rows) T.dup = schedule2(items, NT, opt.target_j, entries);
+        if (opt.adjoint) T.tdup = schedule2(titems, NT, opt.target_j, entries);
       }
       if (kind == WG_NODE_LEAF) {
         std::vector<int> aux(R, 0);
@@ -823,7 +835,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
             if (pg >= 0 && c.nleaves[g] == 1) aux[pg] = 1;
           }
         }
-        T.aux = put_int(P.meta, aux);
+        T.aux = put_int(meta, aux);
       } else if (kind == WG_NODE_WGD) {
         if (T.wa != R) throw Error(WG_EINVAL, "WGD node and its child differ in compatible clades");
         std::vector<Item> items;
@@ -842,7 +854,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
             items.push_back(std::move(it));
           }
         }
-        T.init = schedule2(items, NT, opt.target_j, P.entries);
+        T.init = schedule2(items, NT, opt.target_j, entries);
       } else {
         // speciation + loss (internal) or Πspec + Πloss of the root row
         std::vector<Item> items;
@@ -885,15 +897,15 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
             items.push_back(std::move(it));
           }
         }
-        T.init = schedule2(items, NT, opt.target_j, P.entries);
-        T.loss = put_int2(P.meta, loss);
+        T.init = schedule2(items, NT, opt.target_j, entries);
+        T.loss = put_int2(meta, loss);
         if (opt.adjoint) {
           for (int x = 0; x < T.wa; ++x) ta[x].fa = inva[x] < 0 ? 0xFFFF : inva[x];
           for (int x = 0; x < T.wb; ++x) tb[x].fa = invb[x] < 0 ? 0xFFFF : invb[x];
-          T.ta = schedule2(ta, NT, opt.target_j, P.entries);
-          T.tb = schedule2(tb, NT, opt.target_j, P.entries);
-          T.inva = put_int(P.meta, inva);
-          T.invb = put_int(P.meta, invb);
+          T.ta = schedule2(ta, NT, opt.target_j, entries);
+          T.tb = schedule2(tb, NT, opt.target_j, entries);
+          T.inva = put_int(meta, inva);
+          T.invb = put_int(meta, invb);
         }
       }
       if (kind == WG_NODE_ROOT) {
@@ -934,20 +946,20 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
         if (opt.adjoint)
           for (int x = 0; x < R; ++x) tlw[plevel[x]].push_back(std::move(tby[x]));
         T.nlvl = nl;
-        T.lvl = (int64_t)P.progs.size();
-        for (int L = 0; L < nl; ++L) P.progs.push_back(schedule2(lw[L], NT, opt.target_j, P.entries));
+        T.lvl = (int64_t)tb.progs.size();
+        for (int L = 0; L < nl; ++L) tb.progs.push_back(schedule2(lw[L], NT, opt.target_j, entries));
         if (opt.adjoint) {
-          T.tlvl = (int64_t)P.progs.size();
-          for (int L = 0; L < nl; ++L) P.progs.push_back(schedule2(tlw[L], NT, opt.target_j, P.entries));
+          T.tlvl = (int64_t)tb.progs.size();
+          for (int L = 0; L < nl; ++L) tb.progs.push_back(schedule2(tlw[L], NT, opt.target_j, entries));
         }
-        for (int64_t q = T.lvl; q < (int64_t)P.progs.size(); ++q) T.rslot = std::max(T.rslot, P.progs[q].nslot);
+        for (const DProg2& q : tb.progs) T.rslot = std::max(T.rslot, q.nslot);
       }
       if (kind == WG_NODE_ROOT) {
         // log L outputs: family index and position of its ubiquitous clade
         std::vector<std::array<int, 2>> fam(nf);
         for (int i = 0; i < nf; ++i)
           fam[i] = {opt.global_ids ? (*opt.global_ids)[fams[i]] : fams[i], pos(i, ccds[fams[i]]->n_clades - 1)};
-        T.fam = put_int2(P.meta, fam);
+        T.fam = put_int2(meta, fam);
       }
       // shared memory: cur + nxt rows (children staged in nxt) + slots + spare
       int slots = std::max({T.dup.nslot, T.init.nslot, T.tdup.nslot, T.ta.nslot, T.tb.nslot});
@@ -959,6 +971,57 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       // + the branch's ϕ and ψ rows staged in shared memory
       T.smem = 2 * W2 + slots + 2 * m.nrow[k] + 16 * (NT / 32) + 32;
       const int smem_adj = 6 * W2 + slots + 2 * m.nrow[k] + 16 * (NT / 32) + 32;
+      tb.smem_adj = smem_adj;
+      tb.NT = NT;
+    };
+    std::vector<TaskBuild> builds(groups.size());
+    parallel_for(groups.size(), opt.threads, [&](size_t gi) { build(gi, builds[gi]); });
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+      TaskBuild& tb = builds[gi];
+      DTask T = tb.T;
+      const auto& fams = groups[gi];
+      const int nf = (int)fams.size();
+      const int R = T.width, NT = tb.NT, smem_adj = tb.smem_adj;
+      T.top = P.tops_doubles;
+      P.tops_doubles += R;
+      if (opt.keep_tables) {
+        T.tab = P.tab_doubles;
+        P.tab_doubles += (int64_t)m.nrow[k] * R;
+      }
+      for (int i = 0; i < nf; ++i) {
+        const size_t fk = (size_t)fams[i] * K + k;
+        toploc[fk] = T.top + tb.col[i];
+        P.fam_tab[fk] = T.tab;
+        P.fam_w[fk] = R;
+        P.fam_col[fk] = tb.col[i];
+        P.fam_ncol[fk] = info[fams[i]].ncompat[k];
+      }
+      T.gmap = (int64_t)P.gmap.size();
+      P.gmap.insert(P.gmap.end(), tb.gmap.begin(), tb.gmap.end());
+      // entries, level programs and int tables: task-local offsets made global
+      // (entries are copied once, in parallel, after the last node)
+      const int64_t eb = n_entries;
+      n_entries += (int64_t)tb.entries.size();
+      entry_chunks.push_back(std::move(tb.entries));
+      entry_off.push_back(eb);
+      for (DProg2* pr : {&T.dup, &T.init, &T.tdup, &T.ta, &T.tb}) pr->off += eb, pr->comb += eb;
+      const int64_t pb = (int64_t)P.progs.size();
+      for (DProg2 pr : tb.progs) {
+        pr.off += eb;
+        pr.comb += eb;
+        P.progs.push_back(pr);
+      }
+      T.lvl += pb;
+      T.tlvl += pb;
+      if (P.meta.size() & 1) P.meta.push_back(0);  // int2 tables stay 8-byte aligned
+      const int64_t mb = (int64_t)P.meta.size();
+      P.meta.insert(P.meta.end(), tb.meta.begin(), tb.meta.end());
+      T.aux += mb;
+      T.inva += mb;
+      T.invb += mb;
+      T.loss += mb / 2;
+      T.fam += mb / 2;
+      std::vector<int32_t>().swap(tb.meta);
       if (opt.adjoint) {
         T.gout = P.gout_doubles;
         const int n = m.nrow[k];
@@ -998,6 +1061,12 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       P.tasks.push_back(T);
     }
   }
+  P.entries.resize((size_t)n_entries);
+  parallel_for(entry_chunks.size(), opt.threads, [&](size_t i) {
+    std::vector<DEntry>& c = entry_chunks[i];
+    if (!c.empty()) std::memcpy(P.entries.data() + entry_off[i], c.data(), c.size() * sizeof(DEntry));
+    std::vector<DEntry>().swap(c);
+  });
   // heaviest tasks first inside each launch
   auto by_cost = [&](int a, int b) {
     const DTask& x = P.tasks[a];
