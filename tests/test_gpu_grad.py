@@ -118,3 +118,33 @@ def test_gradient_nowhere_extinct_condition(W, O, ex1_tree, ex1_files):
     otot, og = om.gradient(O.read_ale_files(om, ex1_files), lam, mu, q=[0.25, 0.5], eta=0.72)
     assert tot == pytest.approx(otot, rel=1e-10)
     assert _close(g, og) <= GREL
+
+
+def _slow_rates_case(W, O, lam_mean, mu_mean):
+    from whale_gb300 import synth
+
+    wl = synth.config1(n_families=60)
+    ccds = wl.ccds()
+    keep = [i for i, c in enumerate(ccds) if c.n_clades <= 300][:20]
+    n = len(wl.model.rates.λ)
+    rng = np.random.default_rng(3)
+    lam, mu = rng.normal(np.log(lam_mean), 0.3, n), rng.normal(np.log(mu_mean), 0.3, n)
+    q = np.asarray(wl.model.rates.q)
+    wm = W.WhaleModel(W.DLWGD(λ=lam, μ=mu, q=q, η=0.7), wl.model.tree, wl.model.Δt)
+    g = W.gradient(wm, [ccds[i] for i in keep])
+    om = O.OracleModel(W.nwstr(wm.tree), wm.Δt)
+    otot, og = om.gradient([O.OracleCCD(om, wl.ale[i]) for i in keep], lam, mu, q=q, eta=0.7)
+    return g, og
+
+
+def test_gradient_slow_rates_one_dot_rows(W, O):
+    # λ ~ 0.005, Δt = 0.02: ψ per slice ~ 1e-4, where the one-dot form of the
+    # row adjoints divides a difference of two sums by ψ
+    g, og = _slow_rates_case(W, O, 0.005, 0.004)
+    assert _close(g, og) <= GREL
+
+
+def test_gradient_tiny_duplication_rate_two_dot_rows(W, O):
+    # λ ~ 1e-5: ψ below the one-dot threshold on every branch, the two-dot form
+    g, og = _slow_rates_case(W, O, 1e-5, 0.01)
+    assert _close(g, og) <= GREL

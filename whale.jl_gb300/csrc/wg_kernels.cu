@@ -739,6 +739,41 @@ __device__ __forceinline__ double reduce_scatter16(double (&v)[8], double (&w)[8
   return a[0];
 }
 
+// Warp reduce-scatter of 8 values per lane: afterwards every lane holds the
+// warp sum of value index idx(lane) (lanes differing only in bits 0-1 agree).
+__device__ __forceinline__ double reduce_scatter8(double (&v)[8], int lane, int& idx) {
+  const unsigned FULL = 0xffffffffu;
+  double a[4];
+  const bool hi16 = lane & 16;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const double send = hi16 ? v[i] : v[i + 4];
+    const double keep = hi16 ? v[i + 4] : v[i];
+    a[i] = keep + __shfl_xor_sync(FULL, send, 16);
+  }
+  const bool hi8 = lane & 8;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const double send = hi8 ? a[i] : a[i + 2];
+    const double keep = hi8 ? a[i + 2] : a[i];
+    a[i] = keep + __shfl_xor_sync(FULL, send, 8);
+  }
+  const bool hi4 = lane & 4;
+  {
+    const double send = hi4 ? a[0] : a[1];
+    const double keep = hi4 ? a[1] : a[0];
+    a[0] = keep + __shfl_xor_sync(FULL, send, 4);
+  }
+  a[0] += __shfl_xor_sync(FULL, a[0], 2);
+  a[0] += __shfl_xor_sync(FULL, a[0], 1);
+  idx = (hi16 ? 4 : 0) + (hi8 ? 2 : 0) + (hi4 ? 1 : 0);
+  return a[0];
+}
+
+// Rows with ψ below this take the two-dot form of the row adjoints (the
+// one-dot form divides a difference of two sums by ψ).
+constexpr double kPsiOneDot = 1e-6;
+
 template <int NT>
 __device__ __forceinline__ void block_sum4(double (&v)[4], double* red) {
   for (int o = 16; o > 0; o >>= 1)
@@ -759,14 +794,23 @@ __device__ __forceinline__ void block_sum4(double (&v)[4], double* red) {
 }
 
 // Reverse sweep of one task.  Per-task outputs (gout + T.gout):
-// [2r] ∂/∂ϕ_r, [2r+1] ∂/∂ψ_r (rows r >= 1), [2n] ∂/∂ε_top(child 0),
+// [2r] ∂/∂ϕ_r, [2r+1] ∂/∂ψ_r (rows r >= 1; a branch in the one-dot form of
+// adj_rows writes E_r to [2r] for r = 0..n-1 instead), [2n] ∂/∂ε_top(child 0),
 // [2n+1] ∂/∂ε_top(child 1), [2n+2] ∂/∂q, [2n+3] ∂/∂η, [2n+4] ∂/∂ε_top(own).
 // Reverse rows n-1 .. 1 of a branch.  J > 0: lane program in registers with
 // exactly J iterations; J == 0: entries streamed from memory.  Per row:
 // G[x] = Σ p·bar[γ]·L[sib], bar_{r-1}[x] = ϕ bar[x] + ψ G[x]; then
 // ∂/∂ϕ_r = Σ bar_r·L_{r-1} and ∂/∂ψ_r = ½ Σ G·L_{r-1} (each split counted
-// twice) in a full-lane dot loop, reduced 8 rows at a time by a register-ring
-// reduce-scatter.
+// twice).  The row step is homogeneous of degree 1 in ϕ-terms and 2 in
+// ψ-terms, so with E_r = Σ bar_r·L_r:
+//   E_r = ϕ_r ∂ϕ_r + ψ_r ∂ψ_r,   E_{r-1} = ϕ_r ∂ϕ_r + 2 ψ_r ∂ψ_r,
+// i.e. ∂ψ_r = (E_{r-1} - E_r)/ψ_r and ∂ϕ_r = (2E_r - E_{r-1})/ϕ_r: one dot
+// per row (E_{r-1} = Σ bar_{r-1}·L_{r-1}) instead of two, reduced 8 rows at
+// a time by a register-ring reduce-scatter.  The task writes E_r to out[2r]
+// (r = 0..n-1); the pairs are linear, ϕ and ψ are the node's, so the host
+// forms the row adjoints after the sum over tasks.  Branches with a row whose
+// ψ is below kPsiOneDot (or ϕ = 0) take both dots directly and write
+// ∂/∂ϕ_r, ∂/∂ψ_r to out[2r], out[2r + 1].
 template <int NT, int J>
 __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTask& T, int lane, int n, int R,
                                          const double* phs, const double* pss, double*& bar, double*& barn,
@@ -794,6 +838,24 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
     }
     cp_async_commit();
   };
+  // one-dot form unless a row's ψ is tiny (the choice is uniform over the CTA)
+  bool ok = true;
+  for (int r = 1 + tid; r < n; r += NT) ok &= pss[r] >= kPsiOneDot && phs[r] > 0.0;
+  const bool onedot = __syncthreads_and(ok);
+  constexpr int NW = NT / 32;
+  if (onedot) {  // E_{n-1} = Σ bar_{n-1}·L_{n-1}
+    const double* Ltop = tab0 + (int64_t)(n - 1) * R;
+    double e = 0.0;
+    for (int c = tid; c < R; c += NT) e = fma(bar[c], Ltop[c], e);
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    if (wl == 0) red[wid] = e;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int q = 0; q < NW; ++q) t += red[q];
+      out[2 * (n - 1)] = t;
+    }
+  }
   fetch(n - 1, Lb);
   fetch(n - 2, Lb + W2);
   int bi = 0;
@@ -842,13 +904,36 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
       });
     }
     __syncthreads();
+    const int slot = (n - 1 - r) & 7;
+    if (onedot) {
+      double e = 0.0;  // this lane's share of E_{r-1}
+      for (int c = tid; c < R; c += NT) e = fma(bn[c], Lp[c], e);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) rp[i] = (i == slot) ? e : rp[i];
+      if (slot == 7 || r == 1) {
+        int idx;
+        const double v = reduce_scatter8(rp, wl, idx);
+        if ((wl & 3) == 0) red[8 * wid + idx] = v;
+        __syncthreads();
+        if (tid <= slot) {  // batch slot tid holds E_{rr-1}, rr its row
+          double sum = 0.0;
+          for (int q = 0; q < NW; ++q) sum += red[8 * q + tid];
+          out[2 * (r + slot - tid - 1)] = sum;
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) rp[i] = 0.0;
+      }
+      double* t = bar;
+      bar = barn;
+      barn = t;
+      continue;
+    }
     double dphi = 0.0, dpsi = 0.0;
     for (int c = tid; c < R; c += NT) {
       const double l = Lp[c];
       dphi = fma(bb[c], l, dphi);
       dpsi = fma(Gs[c], l, dpsi);
     }
-    const int slot = (n - 1 - r) & 7;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       rp[i] = (i == slot) ? dphi : rp[i];
@@ -1811,6 +1896,29 @@ void finish_timing(wg_ctx* ctx) {
   ctx->timed = false;
 }
 
+// The adjoint writes, for a branch whose rows all take the one-dot form,
+// E_r = Σ bar_r·L_r per row (summed over tasks into the ∂/∂ϕ slots); the row
+// adjoints follow from consecutive E: ∂ϕ_r = (2E_r - E_{r-1})/ϕ_r and
+// ∂ψ_r = (E_{r-1} - E_r)/ψ_r.  The choice of form repeats the kernel's test.
+void rows_from_sums(const wg_model* m, std::vector<double>& gred) {
+  const int NR = m->total_rows();
+  for (int k = 0; k < m->K; ++k) {
+    const int n = m->nrow[k], o = m->row_off[k];
+    if (m->kind[k] == WG_NODE_ROOT || n < 2) continue;
+    bool onedot = true;
+    for (int r = 1; r < n; ++r) onedot &= m->psi[o + r] >= kPsiOneDot && m->phi[o + r] > 0.0;
+    if (!onedot) continue;
+    double* dp = gred.data() + NR + o;
+    double* ds = gred.data() + 2 * NR + o;
+    for (int r = n - 1; r >= 1; --r) {
+      const double ehi = dp[r], elo = dp[r - 1];
+      dp[r] = (2.0 * ehi - elo) / m->phi[o + r];
+      ds[r] = (elo - ehi) / m->psi[o + r];
+    }
+    dp[0] = 0.0;
+  }
+}
+
 // Per-family log L, the conditioned total and (for a gradient evaluation) the
 // chain from the table adjoints to the rates, on the host.
 // Σ w_f log L_f - c·condition and its gradient; unweighted: w = 1, c = N
@@ -1879,6 +1987,7 @@ void fetch(wg_batch* b, const wg_model* m, double* per_family, double* total, do
     gred.assign(b->h_gred, b->h_gred + b->P);
     for (size_t i = 1; i < b->subs.size(); ++i)
       for (int j = 0; j < b->P; ++j) gred[j] += b->h_gred[i * b->P + j];
+    rows_from_sums(m, gred);
   }
   NwResult nw;
   if (b->nw_pending) {

@@ -1030,6 +1030,8 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
           red[NR + m.row_off[k] + r].push_back(T.gout + 2 * r);
           red[2 * (size_t)NR + m.row_off[k] + r].push_back(T.gout + 2 * r + 1);
         }
+        // row 0's slot: E_0 of the one-dot form of the row adjoints
+        if (n > 1 && kind != WG_NODE_ROOT) red[NR + m.row_off[k]].push_back(T.gout);
         if (ka >= 0) red[eps_top_row(ka)].push_back(T.gout + 2 * n + 0);
         if (kb >= 0) red[eps_top_row(kb)].push_back(T.gout + 2 * n + 1);
         if (kind == WG_NODE_WGD) red[3 * (size_t)NR + k].push_back(T.gout + 2 * n + 2);
