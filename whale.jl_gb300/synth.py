@@ -16,7 +16,7 @@ import math
 import os
 from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass
-from typing import List, Optional
+from typing import List, Optional, Sequence
 
 import numpy as np
 
@@ -88,8 +88,11 @@ class Workload:
 
 
 def simulate_families(wm: WhaleModel, n: int, seed: int, n_trees: int, max_nni: int, min_genes: int = 3,
-                      target_clades: Optional[np.ndarray] = None, walk: bool = False, threads: int = 0) -> List[str]:
-    """ALE texts of ``n`` families simulated on ``wm`` (native, threaded)."""
+                      target_clades: Optional[np.ndarray] = None, walk: bool = False, threads: int = 0,
+                      indices: Optional[Sequence[int]] = None) -> List[str]:
+    """ALE texts of ``n`` families simulated on ``wm`` (native, threaded);
+    with ``indices``, only those families of the ``n`` (each family depends
+    on its index alone)."""
     lam, mu, q, eta, _ = wm.node_rates()
     q = np.where(np.isnan(q), 0.0, q)
     lam = np.where(np.isnan(lam), 0.0, lam)
@@ -114,7 +117,7 @@ def simulate_families(wm: WhaleModel, n: int, seed: int, n_trees: int, max_nni: 
 
     threads = threads or (os.cpu_count() or 4)
     with ThreadPoolExecutor(max_workers=threads) as ex:
-        return list(ex.map(one, range(n)))
+        return list(ex.map(one, range(n) if indices is None else list(indices)))
 
 
 def config0(seed: int = 0, n_families: int = 100) -> Workload:
@@ -157,13 +160,24 @@ def config1(seed: int = 1, n_families: int = 5000) -> Workload:
     return Workload("cfg1", wm, ale, seed, 200, 5)
 
 
-def config4(seed: int = 4, n_families: int = 50000) -> Workload:
+def config4_targets(seed: int = 4, n_families: int = 50000) -> np.ndarray:
+    """Target clade counts of config4's families (Pareto tail, α = 0.8,
+    capped at 20,000)."""
+    rng = np.random.default_rng(seed)
+    _dlwgd_model(40, 10, 0.01, rng)
+    u = rng.uniform(size=n_families)
+    return np.minimum(20000, 10.0 * np.power(1.0 - u, -1.0 / 0.8)).astype(np.int64)
+
+
+def config4(seed: int = 4, n_families: int = 50000, indices: Optional[Sequence[int]] = None) -> Workload:
     """40-taxon Yule tree, Δt=0.01, 10 WGDs, rates as config1; CCDs from 500
-    trees with 0-8 NNIs, heavy-tailed clade counts in [10, 20000]."""
+    trees with 0-8 NNIs, heavy-tailed clade counts in [10, 20000].  With
+    ``indices``, only those families of the 50,000 (identical to theirs in
+    the full workload)."""
     rng = np.random.default_rng(seed)
     wm = _dlwgd_model(40, 10, 0.01, rng)
     u = rng.uniform(size=n_families)
     tgt = np.minimum(20000, 10.0 * np.power(1.0 - u, -1.0 / 0.8)).astype(np.int64)
     ale = simulate_families(wm, n_families, seed, n_trees=500, max_nni=8, min_genes=4, target_clades=tgt,
-                            walk=True)
+                            walk=True, indices=indices)
     return Workload("cfg4", wm, ale, seed, 500, 8)
