@@ -11,9 +11,10 @@ the log-rates by N(0, 0.01²).
   value     families / device time per step (CUDA events around the step's
             device work on the library's stream: parameter upload, forward,
             adjoint, group reduction), families resident in HBM
-  e2e       families / wall time per step of the public API call
-            (logpdf_gradient: slice tables on the host, H2D from pinned memory,
-            kernels, D2H of per-family logL and the gradient, host chain rule)
+  e2e       families / wall time per step of the C-ABI calls a host caller
+            makes with host buffers (wg_model_set_rates: slice tables on the
+            host; wg_logpdf_grad: H2D from pinned memory, kernels, D2H of
+            per-family logL and the gradient, host chain rule)
   --impl reference   the CPU restatement of the reference (forward-mode duals,
             as ForwardDiff) on the host cores, on a bounded sample per step
 
@@ -234,15 +235,32 @@ def main():
     F = W._native.C.c_float
     fms, ams, rms = F(), F(), F()
 
-    def step(m):
-        tot, per, dl, dm, dq, de = batch.grad_nodes(m)
-        W._native.check(L.wg_ctx_timings(ctx.h, W._native.C.byref(fms), W._native.C.byref(ams),
-                                         W._native.C.byref(rms)))
-        return tot, fms.value, ams.value, rms.value
+    # one step through the C ABI, as a ccall caller runs it: the step's per-node
+    # natural rates (host arrays) -> wg_model_set_rates (slice tables on the
+    # host) -> wg_logpdf_grad (H2D from pinned memory, kernels, D2H of the
+    # per-family log L and the gradient, host chain rule) into host buffers
+    N_ = W._native
+    K = len(wm.order)
+    per_b = np.zeros(len(ccds))
+    dl_b, dm_b, dq_b = np.zeros(K), np.zeros(K), np.zeros(K)
+    tot_b, de_b = N_.dbl(), N_.dbl()
+    hm = wm._struct.h
+
+    def step(rates):
+        lam, mu, q, eta, pp = rates
+        N_.check(L.wg_model_set_rates(hm, N_.dptr(lam), N_.dptr(mu), N_.dptr(q), eta, N_.dptr(pp)))
+        N_.check(L.wg_logpdf_grad(ctx.h, hm, batch.h, N_.dptr(per_b), N_.C.byref(tot_b), N_.dptr(dl_b),
+                                  N_.dptr(dm_b), N_.dptr(dq_b), N_.C.byref(de_b), None, None, None))
+        N_.check(L.wg_ctx_timings(ctx.h, N_.C.byref(fms), N_.C.byref(ams), N_.C.byref(rms)))
+        return tot_b.value, fms.value, ams.value, rms.value
+
+    def inputs(m):
+        return tuple(np.ascontiguousarray(x, dtype=np.float64) if isinstance(x, np.ndarray) else float(x)
+                     for x in m.node_rates())
 
     for _ in range(args.warmup):
-        step(perturbed(W, wm, rng))
-    models = [perturbed(W, wm, rng) for _ in range(args.steps)]
+        step(inputs(perturbed(W, wm, rng)))
+    models = [inputs(perturbed(W, wm, rng)) for _ in range(args.steps)]
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
@@ -278,8 +296,11 @@ def main():
     e2e = world * NF / (wall_step_ms * 1e-3)
     NR = wm._struct.total_rows
     K = len(wm.order)
-    h2d = 8 * (3 * NR + K + 1)
-    d2h = 8 * NF + 8 * (3 * NR + K + 1)
+    h2d = 8 * (3 * NR + K + 3)  # slice tables, q, η and the two root-row constants
+    # per-family log L plus one gradient vector per size class of the batch
+    # (clade-count classes bounded at 128, 256, 512, 1024, 1536)
+    n_cls = len({int(np.searchsorted([128, 256, 512, 1024, 1536], c.n_clades, side="left")) for c in ccds})
+    d2h = 8 * NF + 8 * (3 * NR + K + 1) * n_cls
     # forward alone (for the gradient-cost ratio) and the plain one-family-per-launch path
     fwd_only = []
     for _ in range(5):

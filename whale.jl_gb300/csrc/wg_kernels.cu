@@ -1823,6 +1823,12 @@ void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted, bool no
     ck(cudaEventRecordWithFlags(ctx->ev[2], s, cudaEventRecordExternal), "event");
     ck(cudaEventRecordWithFlags(ctx->ev[3], s, cudaEventRecordExternal), "event");
   }
+  // results to the pinned host buffers, inside the graph: fetch only waits
+  ck(cudaMemcpyAsync(b->h_logl, b->d_logl, sizeof(double) * b->NF, cudaMemcpyDeviceToHost, s), "logl download");
+  if (grad)
+    for (size_t i = 0; i < b->subs.size(); ++i)
+      ck(cudaMemcpyAsync(b->h_gred + i * b->P, b->subs[i]->d_gred, sizeof(double) * b->P, cudaMemcpyDeviceToHost, s),
+         "grad download");
 }
 
 // Stage the parameters on the host and replay the captured launch sequence
@@ -1973,13 +1979,8 @@ void finish(const wg_model* m, int NF, const double* logl, const double* gred, b
 void fetch(wg_batch* b, const wg_model* m, double* per_family, double* total, double* d_lam, double* d_mu,
            double* d_q, double* d_eta, double* d_eps, double* d_phi, double* d_psi) {
   cudaStream_t s = b->ctx->stream;
-  ck(cudaMemcpyAsync(b->h_logl, b->d_logl, sizeof(double) * b->NF, cudaMemcpyDeviceToHost, s), "logl download");
   const bool grad = b->grad_pending;
-  if (grad)
-    for (size_t i = 0; i < b->subs.size(); ++i)
-      ck(cudaMemcpyAsync(b->h_gred + i * b->P, b->subs[i]->d_gred, sizeof(double) * b->P, cudaMemcpyDeviceToHost, s),
-         "grad download");
-  ck(cudaStreamSynchronize(s), "evaluation");
+  ck(cudaStreamSynchronize(s), "evaluation");  // the graph ends with the result downloads
   b->pending = false;
   finish_timing(b->ctx);
   std::vector<double> gred;
