@@ -516,8 +516,9 @@ __device__ __forceinline__ double eps_top2(const KArgs2& A, int k) {
   return A.params[A.row_off[k] + A.mnode[k].w - 1];
 }
 
-// Rows 1..n-1 of a branch with the lane program in registers, J exact (no
-// guarded iterations).  cur/nxt are swapped row by row.
+// Rows 1..n-1 of a branch with the lane program in registers: J is the
+// instantiated depth, the program's own depth (lp.J <= J) bounds the
+// iterations.  cur/nxt are swapped row by row.
 template <int NT, bool TABLES, int J>
 __device__ __forceinline__ void fwd_rows(const DEntry* __restrict__ E, const DTask& T, int lane, int n, int R,
                                          const double* phs, const double* pss, double*& cur, double*& nxt,
@@ -579,7 +580,15 @@ __device__ __forceinline__ void fwd_rows_generic(const DEntry* __restrict__ E, c
   }
 }
 
-template <int NT, bool TABLES, int J = 1>
+// Row loops are instantiated for a few program depths only (a program of
+// depth j runs in the smallest instantiation J >= j; the lanes' padding
+// iterations are skipped by a CTA-uniform test): fewer copies of the
+// unrolled loops keep the kernels' instruction footprint small (measured:
+// steps of 2 for the forward rows and 4 for the adjoint rows beat every
+// depth in its own copy by ~5% per evaluation).
+constexpr int kFwdJStep = 2, kAdjJStep = 4;
+
+template <int NT, bool TABLES, int J = kFwdJStep>
 __device__ __forceinline__ bool fwd_rows_dispatch(int j, const DEntry* __restrict__ E, const DTask& T, int lane, int n,
                                                   int R, const double* phs, const double* pss, double*& cur,
                                                   double*& nxt, double* part, double* tab0) {
@@ -587,11 +596,12 @@ __device__ __forceinline__ bool fwd_rows_dispatch(int j, const DEntry* __restric
   if constexpr (J > MAXJ) {
     return false;
   } else {
-    if (j == J) {
+    constexpr int NEXT = (J + kFwdJStep > MAXJ && J < MAXJ) ? MAXJ : J + kFwdJStep;
+    if (j <= J) {
       fwd_rows<NT, TABLES, J>(E, T, lane, n, R, phs, pss, cur, nxt, part, tab0);
       return true;
     }
-    return fwd_rows_dispatch<NT, TABLES, J + 1>(j, E, T, lane, n, R, phs, pss, cur, nxt, part, tab0);
+    return fwd_rows_dispatch<NT, TABLES, NEXT>(j, E, T, lane, n, R, phs, pss, cur, nxt, part, tab0);
   }
 }
 
@@ -797,8 +807,9 @@ __device__ __forceinline__ void block_sum4(double (&v)[4], double* red) {
 // [2r] ∂/∂ϕ_r, [2r+1] ∂/∂ψ_r (rows r >= 1; a branch in the one-dot form of
 // adj_rows writes E_r to [2r] for r = 0..n-1 instead), [2n] ∂/∂ε_top(child 0),
 // [2n+1] ∂/∂ε_top(child 1), [2n+2] ∂/∂q, [2n+3] ∂/∂η, [2n+4] ∂/∂ε_top(own).
-// Reverse rows n-1 .. 1 of a branch.  J > 0: lane program in registers with
-// exactly J iterations; J == 0: entries streamed from memory.  Per row:
+// Reverse rows n-1 .. 1 of a branch.  J > 0: lane program in registers (an
+// instantiation of depth J for programs of depth <= J); J == 0: entries
+// streamed from memory.  Per row:
 // G[x] = Σ p·bar[γ]·L[sib], bar_{r-1}[x] = ϕ bar[x] + ψ G[x]; then
 // ∂/∂ϕ_r = Σ bar_r·L_{r-1} and ∂/∂ψ_r = ½ Σ G·L_{r-1} (each split counted
 // twice).  The row step is homogeneous of degree 1 in ϕ-terms and 2 in
@@ -961,7 +972,7 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
   cp_async_wait<0>();  // only empty groups remain; row 0 reuses the buffers
 }
 
-template <int NT, int J = 1>
+template <int NT, int J = kAdjJStep>
 __device__ __forceinline__ bool adj_rows_dispatch(int j, const DEntry* __restrict__ E, const DTask& T, int lane, int n,
                                                   int R, const double* phs, const double* pss, double*& bar,
                                                   double*& barn, double* Lb, int W2, double* Gs, double* part,
@@ -970,11 +981,12 @@ __device__ __forceinline__ bool adj_rows_dispatch(int j, const DEntry* __restric
   if constexpr (J > MAXJ) {
     return false;
   } else {
-    if (j == J) {
+    constexpr int NEXT = (J + kAdjJStep > MAXJ && J < MAXJ) ? MAXJ : J + kAdjJStep;
+    if (j <= J) {
       adj_rows<NT, J>(E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out);
       return true;
     }
-    return adj_rows_dispatch<NT, J + 1>(j, E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out);
+    return adj_rows_dispatch<NT, NEXT>(j, E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out);
   }
 }
 
