@@ -246,17 +246,22 @@ def main():
     tot_b, de_b = N_.dbl(), N_.dbl()
     hm = wm._struct.h
 
+    # (pointers to the caller's buffers made once, as a compiled caller holds them)
+    out_ptrs = (N_.dptr(per_b), N_.C.byref(tot_b), N_.dptr(dl_b), N_.dptr(dm_b), N_.dptr(dq_b),
+                N_.C.byref(de_b), None, None, None)
+    t_ptrs = (N_.C.byref(fms), N_.C.byref(ams), N_.C.byref(rms))
+
     def step(rates):
-        lam, mu, q, eta, pp = rates
-        N_.check(L.wg_model_set_rates(hm, N_.dptr(lam), N_.dptr(mu), N_.dptr(q), eta, N_.dptr(pp)))
-        N_.check(L.wg_logpdf_grad(ctx.h, hm, batch.h, N_.dptr(per_b), N_.C.byref(tot_b), N_.dptr(dl_b),
-                                  N_.dptr(dm_b), N_.dptr(dq_b), N_.C.byref(de_b), None, None, None))
-        N_.check(L.wg_ctx_timings(ctx.h, N_.C.byref(fms), N_.C.byref(ams), N_.C.byref(rms)))
+        _, lam, mu, q, eta, pp = rates
+        N_.check(L.wg_model_set_rates(hm, lam, mu, q, eta, pp))
+        N_.check(L.wg_logpdf_grad(ctx.h, hm, batch.h, *out_ptrs))
+        N_.check(L.wg_ctx_timings(ctx.h, *t_ptrs))
         return tot_b.value, fms.value, ams.value, rms.value
 
     def inputs(m):
-        return tuple(np.ascontiguousarray(x, dtype=np.float64) if isinstance(x, np.ndarray) else float(x)
-                     for x in m.node_rates())
+        lam, mu, q, eta, pp = m.node_rates()
+        arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (lam, mu, q, pp)]
+        return (arrs, N_.dptr(arrs[0]), N_.dptr(arrs[1]), N_.dptr(arrs[2]), float(eta), N_.dptr(arrs[3]))
 
     for _ in range(args.warmup):
         step(inputs(perturbed(W, wm, rng)))
