@@ -820,9 +820,10 @@ __device__ __forceinline__ void block_sum4(double (&v)[4], double* red) {
 // a time by a register-ring reduce-scatter.  The task writes E_r to out[2r]
 // (r = 0..n-1); the pairs are linear, ϕ and ψ are the node's, so the host
 // forms the row adjoints after the sum over tasks.  Branches with a row whose
-// ψ is below kPsiOneDot (or ϕ = 0) take both dots directly and write
-// ∂/∂ϕ_r, ∂/∂ψ_r to out[2r], out[2r + 1].
-template <int NT, int J>
+// ψ is below kPsiOneDot (or ϕ = 0) take both dots directly (ONEDOT false,
+// entries streamed) and write ∂/∂ϕ_r, ∂/∂ψ_r to out[2r], out[2r + 1].
+// GMEM: the task's rows live in device memory (plain copies, no cp.async).
+template <int NT, int J, bool ONEDOT, bool GMEM>
 __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTask& T, int lane, int n, int R,
                                          const double* phs, const double* pss, double*& bar, double*& barn,
                                          double* Lb, int W2, double* Gs, double* part, double* red,
@@ -838,23 +839,18 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
   // Row r reads table row r-1 from buffer (n-1-r) mod 3 (buffer i at Lb +
   // i·W2); the copies run two rows ahead, one commit group per row (empty
   // past row 1).
-  const bool gmem = T.scratch >= 0;  // rows in device memory: plain copies
   auto fetch = [&](int rr, double* dst) {
     if (rr >= 1) {
       const double* src = tab0 + (int64_t)(rr - 1) * R;
-      if (gmem)
+      if constexpr (GMEM)
         for (int c = tid; c < R; c += NT) dst[c] = src[c];
       else
         for (int c = tid; c < R; c += NT) cp_async8(dst + c, src + c);
     }
     cp_async_commit();
   };
-  // one-dot form unless a row's ψ is tiny (the choice is uniform over the CTA)
-  bool ok = true;
-  for (int r = 1 + tid; r < n; r += NT) ok &= pss[r] >= kPsiOneDot && phs[r] > 0.0;
-  const bool onedot = __syncthreads_and(ok);
   constexpr int NW = NT / 32;
-  if (onedot) {  // E_{n-1} = Σ bar_{n-1}·L_{n-1}
+  if constexpr (ONEDOT) {  // E_{n-1} = Σ bar_{n-1}·L_{n-1}
     const double* Ltop = tab0 + (int64_t)(n - 1) * R;
     double e = 0.0;
     for (int c = tid; c < R; c += NT) e = fma(bar[c], Ltop[c], e);
@@ -916,7 +912,7 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
     }
     __syncthreads();
     const int slot = (n - 1 - r) & 7;
-    if (onedot) {
+    if constexpr (ONEDOT) {
       double e = 0.0;  // this lane's share of E_{r-1}
       for (int c = tid; c < R; c += NT) e = fma(bn[c], Lp[c], e);
 #pragma unroll
@@ -934,36 +930,33 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
 #pragma unroll
         for (int i = 0; i < 8; ++i) rp[i] = 0.0;
       }
-      double* t = bar;
-      bar = barn;
-      barn = t;
-      continue;
-    }
-    double dphi = 0.0, dpsi = 0.0;
-    for (int c = tid; c < R; c += NT) {
-      const double l = Lp[c];
-      dphi = fma(bb[c], l, dphi);
-      dpsi = fma(Gs[c], l, dpsi);
-    }
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      rp[i] = (i == slot) ? dphi : rp[i];
-      rs[i] = (i == slot) ? dpsi : rs[i];
-    }
-    if (slot == 7 || r == 1) {
-      int idx;
-      const double v = reduce_scatter16(rp, rs, wl, idx);
-      if ((wl & 1) == 0) red[16 * wid + idx] = v;
-      __syncthreads();
-      if (tid < 16) {
-        double sum = 0.0;
-        for (int q = 0; q < NT / 32; ++q) sum += red[16 * q + tid];
-        const int i = tid & 7;
-        const int rr = r + slot - i;  // row of batch slot i
-        if (i <= slot) out[2 * rr + (tid >> 3)] = (tid >> 3) ? 0.5 * sum : sum;
+    } else {
+      double dphi = 0.0, dpsi = 0.0;
+      for (int c = tid; c < R; c += NT) {
+        const double l = Lp[c];
+        dphi = fma(bb[c], l, dphi);
+        dpsi = fma(Gs[c], l, dpsi);
       }
 #pragma unroll
-      for (int i = 0; i < 8; ++i) rp[i] = rs[i] = 0.0;
+      for (int i = 0; i < 8; ++i) {
+        rp[i] = (i == slot) ? dphi : rp[i];
+        rs[i] = (i == slot) ? dpsi : rs[i];
+      }
+      if (slot == 7 || r == 1) {
+        int idx;
+        const double v = reduce_scatter16(rp, rs, wl, idx);
+        if ((wl & 1) == 0) red[16 * wid + idx] = v;
+        __syncthreads();
+        if (tid < 16) {
+          double sum = 0.0;
+          for (int q = 0; q < NT / 32; ++q) sum += red[16 * q + tid];
+          const int i = tid & 7;
+          const int rr = r + slot - i;  // row of batch slot i
+          if (i <= slot) out[2 * rr + (tid >> 3)] = (tid >> 3) ? 0.5 * sum : sum;
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) rp[i] = rs[i] = 0.0;
+      }
     }
     double* t = bar;
     bar = barn;
@@ -972,7 +965,7 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
   cp_async_wait<0>();  // only empty groups remain; row 0 reuses the buffers
 }
 
-template <int NT, int J = kAdjJStep>
+template <int NT, bool GMEM, int J = kAdjJStep>
 __device__ __forceinline__ bool adj_rows_dispatch(int j, const DEntry* __restrict__ E, const DTask& T, int lane, int n,
                                                   int R, const double* phs, const double* pss, double*& bar,
                                                   double*& barn, double* Lb, int W2, double* Gs, double* part,
@@ -983,15 +976,15 @@ __device__ __forceinline__ bool adj_rows_dispatch(int j, const DEntry* __restric
   } else {
     constexpr int NEXT = (J + kAdjJStep > MAXJ && J < MAXJ) ? MAXJ : J + kAdjJStep;
     if (j <= J) {
-      adj_rows<NT, J>(E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out);
+      adj_rows<NT, J, true, GMEM>(E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out);
       return true;
     }
-    return adj_rows_dispatch<NT, NEXT>(j, E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out);
+    return adj_rows_dispatch<NT, GMEM, NEXT>(j, E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out);
   }
 }
 
 // ROOT as for k_fwd2.  Four 128-thread CTAs per SM leave the adjoint its
-// ~120 registers: at five or six the spills cost more than the occupancy
+// ~110 registers: at five or six the spills cost more than the occupancy
 // gains (the rows are latency-bound, not FP64-bound).
 template <int NT, bool ROOT = false, bool GLOBAL = false>
 __global__ void __launch_bounds__(NT, NT == 128 && !GLOBAL ? 4 : (GLOBAL ? 1 : 2))
@@ -1134,8 +1127,14 @@ __global__ void __launch_bounds__(NT, NT == 128 && !GLOBAL ? 4 : (GLOBAL ? 1 : 2
     }
     __syncthreads();
     const double* tab0 = A.tabs + T.tab;
-    if (!adj_rows_dispatch<NT>(T.tdup.J, E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red, tab0, out))
-      adj_rows<NT, 0>(E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red, tab0, out);
+    // one-dot row adjoints unless a row's ψ is tiny (uniform over the CTA)
+    bool ok = true;
+    for (int r = 1 + tid; r < n; r += NT) ok &= pss[r] >= kPsiOneDot && phs[r] > 0.0;
+    if (!__syncthreads_and(ok))
+      adj_rows<NT, 0, false, GLOBAL>(E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red, tab0, out);
+    else if (!adj_rows_dispatch<NT, GLOBAL>(T.tdup.J, E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red,
+                                           tab0, out))
+      adj_rows<NT, 0, true, GLOBAL>(E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red, tab0, out);
   }
   __syncthreads();
   // ---- row 0
