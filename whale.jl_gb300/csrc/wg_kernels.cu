@@ -880,7 +880,7 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
       if (active)
         rows_reg<(J > 0 ? J : 1), op::FIN_ADJ>(lp, bb, Lp, part, ph, ps, [&](unsigned c, double v, double g) {
           bn[c] = v;
-          Gs[c] = g;
+          if constexpr (!ONEDOT) Gs[c] = g;  // G is read by the two-dot form only
         });
     } else if (active) {
       const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + td.off) + lane;
@@ -894,7 +894,7 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
           acc = v;
         } else if (fin) {
           bn[x.f0] = v;
-          Gs[x.f0] = acc;
+          if constexpr (!ONEDOT) Gs[x.f0] = acc;
           acc = 0.0;
         } else if (x.opc == op::FIN_PART) {
           part[x.f2] = acc;
@@ -907,7 +907,7 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
       // (combine entries stream from memory here: registers are the limit)
       run_comb<NT>(E, td, part, [&](unsigned, unsigned c, unsigned, unsigned, double g) {
         bn[c] = fma(ps, g, ph * bb[c]);
-        Gs[c] = g;
+        if constexpr (!ONEDOT) Gs[c] = g;
       });
     }
     __syncthreads();
