@@ -1084,18 +1084,15 @@ __global__ void __launch_bounds__(NT, NT == 128 && !GLOBAL ? 4 : (GLOBAL ? 1 : 2
     auto afin = [&](unsigned, unsigned x, unsigned fa, unsigned, double acc) {
       A.bartops[gm[x]] = acc + (fa != 0xFFFFu ? bbc[fa] * eb : 0.0);
     };
+    // ta and tb have disjoint partial slots: one combine phase after both
     run_any(E, T.ta, lane, bbc, Y, part, afin);
-    if (T.ta.ncomb) {
-      __syncthreads();
-      run_comb<NT>(E, T.ta, part, afin);
-    }
-    __syncthreads();
     auto bfin = [&](unsigned, unsigned x, unsigned fa, unsigned, double acc) {
       A.bartops[gm[T.wa + x]] = acc + (fa != 0xFFFFu ? bbc[fa] * ea : 0.0);
     };
     run_any(E, T.tb, lane, bbc, X, part, bfin);
-    if (T.tb.ncomb) {
+    if (T.ta.ncomb || T.tb.ncomb) {
       __syncthreads();
+      run_comb<NT>(E, T.ta, part, afin);
       run_comb<NT>(E, T.tb, part, bfin);
     }
     block_sum4<NT>(acc4, red);
@@ -1181,18 +1178,15 @@ __global__ void __launch_bounds__(NT, NT == 128 && !GLOBAL ? 4 : (GLOBAL ? 1 : 2
     auto afin = [&](unsigned, unsigned x, unsigned fa, unsigned, double acc) {
       A.bartops[gm[x]] = acc + (fa != 0xFFFFu ? bar[fa] * eb : 0.0);
     };
+    // ta and tb have disjoint partial slots: one combine phase after both
     run_any(E, T.ta, lane, bar, Y, part, afin);
-    if (T.ta.ncomb) {
-      __syncthreads();
-      run_comb<NT>(E, T.ta, part, afin);
-    }
-    __syncthreads();
     auto bfin = [&](unsigned, unsigned x, unsigned fa, unsigned, double acc) {
       A.bartops[gm[T.wa + x]] = acc + (fa != 0xFFFFu ? bar[fa] * ea : 0.0);
     };
     run_any(E, T.tb, lane, bar, X, part, bfin);
-    if (T.tb.ncomb) {
+    if (T.ta.ncomb || T.tb.ncomb) {
       __syncthreads();
+      run_comb<NT>(E, T.ta, part, afin);
       run_comb<NT>(E, T.tb, part, bfin);
     }
     double acc4[4] = {0.0, 0.0, 0.0, 0.0};  // dea, deb

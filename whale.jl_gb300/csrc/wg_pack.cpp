@@ -546,7 +546,9 @@ inline double bits_to_double(uint64_t b) {
 // Lane programs with fused finalize.  An item (one clade) is its products
 // followed by its finalize op; items longer than J ops are split into
 // segments ending in FIN_PART, finished by a combine entry after a barrier.
-DProg2 schedule2(std::vector<Item>& items, int ntmax, int target_j, std::vector<DEntry>& out) {
+// Partial slots are numbered from slot_base (a program run right after
+// another without a barrier takes slots after the other's).
+DProg2 schedule2(std::vector<Item>& items, int ntmax, int target_j, std::vector<DEntry>& out, int slot_base = 0) {
   DProg2 pr;
   pr.off = (int64_t)out.size();
   int64_t W = 0;
@@ -609,8 +611,8 @@ DProg2 schedule2(std::vector<Item>& items, int ntmax, int target_j, std::vector<
   std::vector<int> slot0(items.size(), -1);
   int nslot = 0;
   for (int i = 0; i < (int)items.size(); ++i)
-    if (nseg[i] > 1) { slot0[i] = nslot; nslot += nseg[i]; }
-  if (nslot >= 65535) throw Error(WG_ERANGE, "program exceeds 65535 partial slots");
+    if (nseg[i] > 1) { slot0[i] = slot_base + nslot; nslot += nseg[i]; }
+  if (slot_base + nslot >= 65535) throw Error(WG_ERANGE, "program exceeds 65535 partial slots");
   int used = 0;
   for (int b = 0; b < NB; ++b) if (!bins[b].empty()) used = b + 1;
   const int nt = ((used + 31) / 32) * 32;
@@ -903,7 +905,8 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
           for (int x = 0; x < T.wa; ++x) ta[x].fa = inva[x] < 0 ? 0xFFFF : inva[x];
           for (int x = 0; x < T.wb; ++x) tb[x].fa = invb[x] < 0 ? 0xFFFF : invb[x];
           T.ta = schedule2(ta, NT, opt.target_j, entries);
-          T.tb = schedule2(tb, NT, opt.target_j, entries);
+          // the adjoint runs tb straight after ta: disjoint partial slots
+          T.tb = schedule2(tb, NT, opt.target_j, entries, T.ta.nslot);
           T.inva = put_int(meta, inva);
           T.invb = put_int(meta, invb);
         }
@@ -962,7 +965,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
         T.fam = put_int2(meta, fam);
       }
       // shared memory: cur + nxt rows (children staged in nxt) + slots + spare
-      int slots = std::max({T.dup.nslot, T.init.nslot, T.tdup.nslot, T.ta.nslot, T.tb.nslot});
+      int slots = std::max({T.dup.nslot, T.init.nslot, T.tdup.nslot, T.ta.nslot + T.tb.nslot});
       slots = std::max(slots, T.rslot);  // root: the level programs' partial slots
       // forward: cur, nxt (children staged in nxt); adjoint: bar, barn, two
       // L rows, G; then partial slots and reduction scratch
