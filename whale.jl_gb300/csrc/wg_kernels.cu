@@ -460,7 +460,7 @@ __device__ __forceinline__ void rows_reg(const LaneProg<MAXJ>& lp, const double*
 // finalize op FIN).  Levels are short and latency-bound, so each level's
 // first kLvlJ entries per lane, its first combine entry per thread and the
 // descriptor of the level after it are loaded while the level before it
-// runs; entries past kLvlJ stream from memory.  comb(opc, c, fa, fb, s)
+// runs; entries past kLvlJ are prefetched to L1 then.  comb(opc, c, fa, fb, s)
 // finishes split clades after a barrier.  wl: lane in the program, tix:
 // thread index among the NTG.
 constexpr int kLvlJ = 4;
@@ -488,6 +488,8 @@ __device__ __forceinline__ void chain_levels(const DEntry* __restrict__ E, const
       load_lane_prog<kLvlJ>(E, nxt, wl, lpn);
       crn = load_comb(E, nxt, tix);
       if (i + 2 < nlvl) nn = progs[at(i + 2)];
+      if (wl < nxt.nt)  // the next level's entries past the registers, to L1
+        for (int j = kLvlJ; j < nxt.J; ++j) prefetch_l1(E + nxt.off + (size_t)j * nxt.nt + wl);
     }
     if (wl < cur.nt) {
       double acc = 0.0;
