@@ -241,3 +241,26 @@ def test_packing_does_not_depend_on_host_threads(W, monkeypatch):
     one = summary()
     monkeypatch.setenv("WG_PACK_THREADS", "5")
     assert np.array_equal(one, summary())
+
+
+def test_ale_parser_whitespace_forms(W, O, ex1_tree, ex1_files):
+    # CRLF line ends and extra blanks around the set-id separator parse as
+    # the original text; a ":\t" glued to the set id takes the reference's
+    # literal deletion (src/ccd.jl:154), which merges the id with the first
+    # leaf: the library and the oracle both reject that file
+    t = W.readnw(ex1_tree)
+    wm = W.WhaleModel(W.DLWGD(λ=np.ones(17), μ=np.ones(17), q=[0.2, 0.1], η=0.9), t, 0.05)
+    text = read(ex1_files[0])
+    ref = W.parse_ale_text(text, wm).arrays()
+    i = text.index("#set-id")
+    j = text.index("#", i + 1)
+    for variant in (text.replace("\n", "\r\n"),
+                    text[:i] + text[i:j].replace("\t:\t", "  \t:\t  ") + text[j:]):
+        a = W.parse_ale_text(variant, wm).arrays()
+        assert all(np.array_equal(a[k], ref[k]) for k in ref)
+    glued = text[:i] + text[i:j].replace("\t:\t", ":\t", 3) + text[j:]
+    with pytest.raises(W.WhaleError):
+        W.parse_ale_text(glued, wm)
+    om = O.OracleModel(ex1_tree, 0.05)
+    with pytest.raises(Exception):
+        O.OracleCCD(om, glued)
