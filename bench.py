@@ -169,8 +169,11 @@ def run_reference(args, W, rank):
 
     wl = synth.config1(n_families=args.families)
     threads = os.cpu_count() or 1
-    # each step a bounded sample, large enough to keep every host thread busy
-    idx = pick_cpu_sample(W, wl, max(0.5, args.cpu_budget / max(1, args.steps + args.warmup)), threads)
+    # each step a bounded sample: the whole run about two minutes of CPU work
+    # (at most 0.5 s per step; at 1,000 steps still ~800 families per step,
+    # enough to keep every host thread busy)
+    per_step = max(0.03, min(0.5, 120.0 / max(1, args.steps + args.warmup)))
+    idx = pick_cpu_sample(W, wl, per_step, threads)
     v, times = cpu_reference(W, wl, idx, args.steps, args.warmup, threads)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
