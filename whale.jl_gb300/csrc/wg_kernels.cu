@@ -865,19 +865,10 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
       out[2 * (n - 1)] = t;
     }
   }
-  fetch(n - 1, Lb);
-  fetch(n - 2, Lb + W2);
-  int bi = 0;
-  for (int r = n - 1; r >= 1; --r) {
-    double* Lp = Lb + bi * W2;
-    cp_async_wait<1>();
-    __syncthreads();
-    // every thread is past row r+1, whose buffer takes table row r-3
-    fetch(r - 2, Lb + (bi == 0 ? 2 : bi - 1) * W2);
-    bi = bi == 2 ? 0 : bi + 1;
+  // One row's program and split-clade combines: bar_{r-1} into bn from bar_r
+  // (bb) and table row r-1 (Lp).
+  auto row = [&](int r, const double* Lp, const double* bb, double* bn) {
     const double ph = phs[r], ps = pss[r];
-    double* bn = barn;
-    const double* bb = bar;
     if (J > 0) {
       if (active)
         rows_reg<(J > 0 ? J : 1), op::FIN_ADJ>(lp, bb, Lp, part, ph, ps, [&](unsigned c, double v, double g) {
@@ -912,9 +903,27 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
         if constexpr (!ONEDOT) Gs[c] = g;
       });
     }
+  };
+  int bi = 0;
+  fetch(n - 1, Lb);
+  fetch(n - 2, Lb + W2);
+  if constexpr (ONEDOT) {
+    // One CTA barrier per row: it follows the program (bar_{r-1} complete)
+    // once each thread's copies of the next row's table row have landed.
+    // The dot reads only bar_{r-1} and row r-1, which the next program does
+    // not write, and a buffer is refilled only after the barrier that
+    // follows its last reader (the dot of the row above).
+    cp_async_wait<1>();
     __syncthreads();
-    const int slot = (n - 1 - r) & 7;
-    if constexpr (ONEDOT) {
+    for (int r = n - 1; r >= 1; --r) {
+      double* Lp = Lb + bi * W2;
+      double* bn = barn;
+      row(r, Lp, bar, bn);
+      cp_async_wait<0>();
+      __syncthreads();
+      fetch(r - 2, Lb + (bi == 0 ? 2 : bi - 1) * W2);  // row r+1's buffer takes table row r-3
+      bi = bi == 2 ? 0 : bi + 1;
+      const int slot = (n - 1 - r) & 7;
       double e = 0.0;  // this lane's share of E_{r-1}
       for (int c = tid; c < R; c += NT) e = fma(bn[c], Lp[c], e);
 #pragma unroll
@@ -932,7 +941,22 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
 #pragma unroll
         for (int i = 0; i < 8; ++i) rp[i] = 0.0;
       }
-    } else {
+      double* t = bar;
+      bar = barn;
+      barn = t;
+    }
+  } else {
+    for (int r = n - 1; r >= 1; --r) {
+      double* Lp = Lb + bi * W2;
+      cp_async_wait<1>();
+      __syncthreads();
+      // every thread is past row r+1, whose buffer takes table row r-3
+      fetch(r - 2, Lb + (bi == 0 ? 2 : bi - 1) * W2);
+      bi = bi == 2 ? 0 : bi + 1;
+      const double* bb = bar;
+      row(r, Lp, bb, barn);
+      __syncthreads();
+      const int slot = (n - 1 - r) & 7;
       double dphi = 0.0, dpsi = 0.0;
       for (int c = tid; c < R; c += NT) {
         const double l = Lp[c];
@@ -959,10 +983,10 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
 #pragma unroll
         for (int i = 0; i < 8; ++i) rp[i] = rs[i] = 0.0;
       }
+      double* t = bar;
+      bar = barn;
+      barn = t;
     }
-    double* t = bar;
-    bar = barn;
-    barn = t;
   }
   cp_async_wait<0>();  // only empty groups remain; row 0 reuses the buffers
 }
