@@ -104,7 +104,7 @@ class ClockSampler:
 # DRAM bytes per evaluation of the 5,000-family workload, summed over the
 # launches of each kernel family, from the ncu launch list kept in
 # profiles/launches_cfg1_5000fam.txt (not measurable inside the timed run).
-NCU_DRAM_BYTES = {"adjoint": 758_560_256, "forward": 349_633_024}
+NCU_DRAM_BYTES = {"adjoint": 758_141_440, "forward": 349_668_352}
 
 
 def workload(nf):
