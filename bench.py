@@ -175,6 +175,9 @@ def run_reference(args, W, rank):
     per_step = max(0.03, min(0.5, 120.0 / max(1, args.steps + args.warmup)))
     idx = pick_cpu_sample(W, wl, per_step, threads)
     v, times = cpu_reference(W, wl, idx, args.steps, args.warmup, threads)
+    # the same on one core, for the single-thread figure (a smaller sample)
+    idx1 = pick_cpu_sample(W, wl, 2.0, 1)
+    v1, _ = cpu_reference(W, wl, idx1, 1, 0, 1)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True,
@@ -185,6 +188,8 @@ def run_reference(args, W, rank):
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{len(idx)} of {args.families} families (random, seed 7) per step"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_one_core": {"value": v1, "unit": UNIT, "cores": 1,
+                         "sample": f"{len(idx1)} of {args.families} families (random, seed 7), one step"},
         "note": "Julia is not available, so the reference itself cannot run; this is the C++ restatement "
                 "of its logpdf + ForwardDiff gradient (oracle/whale_oracle.cpp), OpenMP over families",
     }
