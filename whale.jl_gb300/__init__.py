@@ -16,6 +16,7 @@ from .ccd import CCD, parse_ale_text, read_ale
 from .core import (Batch, Context, default_context, get_batch, gradient, logpdf, logpdf_gradient, logpdf_inplace,
                    logpdf_plain, loglikelihood, map_gradient, nowhere_condition)
 from .mixture import MixtureModel, ModelArray
+from .autotune import tune
 from .track import RecNode, RecTree, backtrack
 from .model import (ConstantDLWGD, DLWGD, NoCondition, NonExtinctCondition, NowhereExtinctCondition, RootCondition,
                     WhaleModel, condition)
@@ -31,5 +32,5 @@ __all__ = [
     "logpdf_gradient", "logpdf_plain", "map_gradient", "Batch", "Context", "default_context", "get_batch",
     "readnw", "nwstr", "insertnode", "getlca", "getleaves", "getroot", "postwalk", "prewalk", "extree", "EXTREE",
     "addbranchwgds", "copytree", "Node", "WhaleError", "MixtureModel", "ModelArray", "backtrack", "RecNode",
-    "RecTree",
+    "RecTree", "tune",
 ]

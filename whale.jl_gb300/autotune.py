@@ -1,0 +1,138 @@
+"""Autotuner for the packed layout of one workload.
+
+The packer's knobs decide how a batch maps onto the GPU:
+
+  target_ops  product + finalize operations per row a task aims for
+              (families per task, hence CTAs per launch and row width)
+  target_j    iterations per row a lane program aims for (lanes per task)
+  root_group  root tasks take target_ops x root_group operations (all split
+              levels together): how many families share a root task
+  heavy_ops   operations per row above which a non-root task gets 256
+              threads instead of 128
+
+``tune(wm, ccds)`` builds the batch under candidate settings, times a few
+evaluations of each on the device (CUDA events around the launch sequence,
+the same clock as ``bench.py``'s ``value``) and keeps the fastest, by
+coordinate descent from the library's defaults: each knob in turn tries its
+neighbours with the others fixed, and a move is kept only if it is faster by
+more than ``min_gain``.  The result is the best setting and its batch, ready
+for evaluations.  Every setting gives the same log-likelihood and gradient
+to rounding; only the layout and the time change.
+
+The knobs reach the packer through environment variables (WG_PACK_TARGET_OPS,
+WG_PACK_TARGET_J, WG_PACK_ROOT_GROUP, WG_PACK_HEAVY_OPS), set only while a
+candidate batch is built.
+"""
+from __future__ import annotations
+
+import contextlib
+import os
+import threading
+from typing import Callable, Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _native as N
+
+DEFAULTS: Dict[str, int] = {"target_ops": 480, "target_j": 3, "root_group": 16, "heavy_ops": 1024}
+NEIGHBOURS: Dict[str, Tuple[int, ...]] = {
+    "target_ops": (240, 320, 480, 720, 960),
+    "target_j": (2, 3, 4, 5),
+    "root_group": (4, 8, 16, 32),
+    "heavy_ops": (512, 1024, 2048),
+}
+_ENV = {"target_ops": "WG_PACK_TARGET_OPS", "target_j": "WG_PACK_TARGET_J", "root_group": "WG_PACK_ROOT_GROUP",
+        "heavy_ops": "WG_PACK_HEAVY_OPS"}
+_env_lock = threading.Lock()
+
+
+@contextlib.contextmanager
+def packing(setting: Dict[str, int]):
+    """Batches created inside use the given packer knobs."""
+    with _env_lock:
+        old = {k: os.environ.get(v) for k, v in _ENV.items()}
+        try:
+            for k, v in setting.items():
+                if k not in _ENV:
+                    raise KeyError(f"unknown packing knob {k!r}")
+                os.environ[_ENV[k]] = str(int(v))
+            yield
+        finally:
+            for k, v in old.items():
+                if v is None:
+                    os.environ.pop(_ENV[k], None)
+                else:
+                    os.environ[_ENV[k]] = v
+
+
+def _descend(measure: Callable[[Dict[str, int]], float], start: Dict[str, int],
+             neighbours: Dict[str, Sequence[int]], min_gain: float, rounds: int) -> Tuple[Dict[str, int], float, List]:
+    best = dict(start)
+    best_t = measure(best)
+    log = [(dict(best), best_t)]
+    seen = {tuple(sorted(best.items())): best_t}
+    for _ in range(rounds):
+        moved = False
+        for knob, values in neighbours.items():
+            for v in values:
+                if v == best[knob]:
+                    continue
+                cand = dict(best)
+                cand[knob] = v
+                key = tuple(sorted(cand.items()))
+                if key not in seen:
+                    seen[key] = measure(cand)
+                    log.append((dict(cand), seen[key]))
+                if seen[key] < best_t * (1.0 - min_gain):
+                    best, best_t, moved = cand, seen[key], True
+        if not moved:
+            break
+    return best, best_t, log
+
+
+def tune(wm, ccds: Sequence, grad: bool = True, steps: int = 5, warmup: int = 2, ctx=None,
+         neighbours: Optional[Dict[str, Sequence[int]]] = None, min_gain: float = 0.01, rounds: int = 2,
+         measure: Optional[Callable[[Dict[str, int]], float]] = None):
+    """Fastest packing of ``ccds`` for ``wm`` (gradient evaluations when
+    ``grad``).  Returns ``(setting, batch, log)``: the knob values, the batch
+    built with them (None when ``measure`` is given), and every
+    (setting, ms per evaluation) tried.  ``measure`` replaces the device
+    timing (a function of the setting returning milliseconds)."""
+    from .core import Batch, default_context
+
+    neighbours = dict(NEIGHBOURS if neighbours is None else neighbours)
+    if measure is not None:
+        best, _, log = _descend(measure, DEFAULTS, neighbours, min_gain, rounds)
+        return best, None, log
+    ctx = ctx or default_context()
+    L = N.lib()
+    N.check(L.wg_ctx_set_timing(ctx.h, 1))
+    f, a, r = N.C.c_float(), N.C.c_float(), N.C.c_float()
+    kept = {"key": None, "ms": float("inf"), "batch": None}  # the fastest batch so far only
+
+    def device_ms(setting):
+        with packing(setting):
+            b = Batch(wm, ccds, grad=grad, ctx=ctx)
+        times = []
+        for i in range(warmup + steps):
+            if grad:
+                b.grad_nodes(wm)
+                N.check(L.wg_ctx_timings(ctx.h, N.C.byref(f), N.C.byref(a), N.C.byref(r)))
+                t = f.value + a.value + r.value
+            else:
+                b.logpdf(wm)
+                N.check(L.wg_ctx_timings(ctx.h, N.C.byref(f), None, None))
+                t = f.value
+            if i >= warmup:
+                times.append(t)
+        ms = float(np.median(times))
+        if ms < kept["ms"]:
+            kept.update(key=tuple(sorted(setting.items())), ms=ms, batch=b)
+        return ms
+
+    best, _, log = _descend(device_ms, DEFAULTS, neighbours, min_gain, rounds)
+    if kept["key"] != tuple(sorted(best.items())):
+        kept["batch"] = None
+        with packing(best):
+            kept["batch"] = Batch(wm, ccds, grad=grad, ctx=ctx)
+    return best, kept["batch"], log

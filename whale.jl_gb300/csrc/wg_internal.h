@@ -30,6 +30,17 @@ inline int default_host_threads() {
   return e ? std::atoi(e) : 0;
 }
 
+// A packing knob from the environment (WG_PACK_TARGET_OPS, WG_PACK_TARGET_J,
+// WG_PACK_ROOT_GROUP, WG_PACK_HEAVY_OPS: what the autotuner varies), else
+// its default; values outside [lo, hi] are refused.
+inline int64_t pack_knob(const char* name, int64_t dflt, int64_t lo, int64_t hi) {
+  const char* e = std::getenv(name);
+  if (!e || !*e) return dflt;
+  const long long v = std::atoll(e);
+  if (v < lo || v > hi) throw Error(WG_EINVAL, std::string(name) + " out of range");
+  return (int64_t)v;
+}
+
 // fn(i) for i < n on up to `threads` host threads (0: all cores); the first
 // exception is rethrown here.
 template <class F>
@@ -304,18 +315,18 @@ constexpr int kNT2L = 128;   // threads per CTA of light tasks
 constexpr int kNT2H = 256;   // threads per CTA of heavy (single large family) tasks
 
 struct PackOptions2 {
-  int64_t target_ops = 480;   // forward product + finalize ops per row per task
-  int64_t heavy_ops = 1024;   // non-root tasks above this many ops per row get kNT2H threads
+  int64_t target_ops = pack_knob("WG_PACK_TARGET_OPS", 480, 32, 1 << 16);  // forward product + finalize ops per row per task
+  int64_t heavy_ops = pack_knob("WG_PACK_HEAVY_OPS", 1024, 32, 1 << 20);  // non-root tasks above this many ops per row get kNT2H threads
   int64_t max_width = 6144;   // cap on a task's row width
   // Root tasks run their same-row levels one after another, each short and
   // latency-bound, so they take target_ops * root_group ops (all levels
   // together), up to max_width_root clades (their adjoint keeps six rows).
-  int root_group = 16;
+  int root_group = (int)pack_knob("WG_PACK_ROOT_GROUP", 16, 1, 256);
   int64_t max_width_root = 1536;
   // tasks needing more shared doubles than this keep their working rows in
   // device memory (L2-resident) instead
   int64_t smem_limit_doubles = 227 * 1024 / 8;
-  int target_j = 3;           // iterations per row the lane scheduler aims for
+  int target_j = (int)pack_knob("WG_PACK_TARGET_J", 3, 1, 16);  // iterations per row the lane scheduler aims for
   bool keep_tables = false;
   bool adjoint = false;
   const std::vector<int>* global_ids = nullptr;  // family index written to log L outputs
