@@ -7,9 +7,12 @@
 #include <cstdint>
 #include <cstdlib>
 #include <exception>
+#include <memory>
+#include <new>
 #include <stdexcept>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "../../include/whalegpu.h"
@@ -143,6 +146,22 @@ constexpr uint64_t kEnd = 2;
 struct alignas(16) DEntry {
   uint64_t code;  // a | b << 16 | dst << 32 | flags << 48
   double p;
+};
+
+// Allocator whose resize() leaves trivial elements uninitialised: large
+// buffers that are filled right after (in parallel) are not first zeroed on
+// one thread.
+template <class T>
+struct UninitAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind { using other = UninitAlloc<U>; };
+  UninitAlloc() = default;
+  template <class U>
+  UninitAlloc(const UninitAlloc<U>&) noexcept {}
+  template <class U>
+  void construct(U* p) noexcept { ::new ((void*)p) U; }
+  template <class U, class... A>
+  void construct(U* p, A&&... a) { ::new ((void*)p) U(std::forward<A>(a)...); }
 };
 
 struct DProg {
@@ -288,7 +307,7 @@ struct DTask {
 
 struct Packed2 {
   std::vector<DTask> tasks;
-  std::vector<DEntry> entries;
+  std::vector<DEntry, UninitAlloc<DEntry>> entries;  // filled in parallel after sizing
   std::vector<int32_t> meta;
   std::vector<int64_t> gmap;
   std::vector<DProg2> progs;               // level programs

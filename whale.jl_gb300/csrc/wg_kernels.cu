@@ -1264,8 +1264,8 @@ T* dalloc(size_t n, int64_t& bytes) {
   return static_cast<T*>(p);
 }
 
-template <class T>
-void h2d(T* d, const std::vector<T>& h, cudaStream_t s) {
+template <class T, class A>
+void h2d(T* d, const std::vector<T, A>& h, cudaStream_t s) {
   if (!h.empty()) ck(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
 }
 

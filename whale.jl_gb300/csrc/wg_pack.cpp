@@ -529,7 +529,47 @@ struct Item {
   int c = 0;                  // output position of the finalize op
   uint32_t fin = op::FIN_DUP;
   int fa = 0xFFFF, fb = 0xFFFF;
-  std::vector<Ent> prods;
+};
+
+// Items with their products in CSR form: item i's products are
+// ents[off[i] .. off[i + 1]), in the order they were added.
+struct ItemList {
+  std::vector<Item> items;
+  std::vector<int64_t> off{0};
+  std::vector<Ent> ents;
+  int size() const { return (int)items.size(); }
+  int nprod(int i) const { return (int)(off[i + 1] - off[i]); }
+  void open(const Item& it) { items.push_back(it); }
+  void prod(int a, int b, double p) { ents.push_back({a, b, p}); }
+  void close() { off.push_back((int64_t)ents.size()); }
+};
+
+// Products addressed to items by index as they arrive (the transposed
+// programs of the adjoint); finish() sorts them by item, stably, so each
+// item keeps its products in arrival order.
+struct ScatterList {
+  std::vector<Item> items;
+  std::vector<int> to;
+  std::vector<Ent> ents;
+  explicit ScatterList(int n = 0) : items(n) {}
+  void add(int x, int a, int b, double p) {
+    to.push_back(x);
+    ents.push_back({a, b, p});
+  }
+  ItemList finish() {
+    ItemList L;
+    const int n = (int)items.size();
+    L.items = std::move(items);
+    L.off.assign((size_t)n + 1, 0);
+    for (int x : to) ++L.off[(size_t)x + 1];
+    for (int i = 0; i < n; ++i) L.off[i + 1] += L.off[i];
+    std::vector<int64_t> cur(L.off.begin(), L.off.end() - 1);
+    L.ents.resize(ents.size());
+    for (size_t j = 0; j < to.size(); ++j) L.ents[cur[to[j]]++] = ents[j];
+    std::vector<int>().swap(to);
+    std::vector<Ent>().swap(ents);
+    return L;
+  }
 };
 
 inline uint64_t pack_code(uint32_t f0, uint32_t f1, uint32_t f2, uint32_t opc) {
@@ -543,35 +583,47 @@ inline double bits_to_double(uint64_t b) {
   return d;
 }
 
+inline int first_set(const uint64_t* w, int nw) {
+  for (int i = 0; i < nw; ++i)
+    if (w[i]) return 64 * i + __builtin_ctzll(w[i]);
+  return -1;
+}
+
 // Lane programs with fused finalize.  An item (one clade) is its products
 // followed by its finalize op; items longer than J ops are split into
 // segments ending in FIN_PART, finished by a combine entry after a barrier.
-// Partial slots are numbered from slot_base (a program run right after
-// another without a barrier takes slots after the other's).
-DProg2 schedule2(std::vector<Item>& items, int ntmax, int target_j, std::vector<DEntry>& out, int slot_base = 0) {
+// Segments go longest first (ties in item order) to the first lane with
+// room for them (first-fit decreasing into lanes of J ops); J grows until
+// they fit.  Partial slots are numbered from slot_base (a program run right
+// after another without a barrier takes slots after the other's).
+DProg2 schedule2(const ItemList& items, int ntmax, int target_j, std::vector<DEntry>& out, int slot_base = 0) {
   DProg2 pr;
   pr.off = (int64_t)out.size();
+  const int n = items.size();
   int64_t W = 0;
   int maxops = 0;
-  for (auto& it : items) {
-    W += (int64_t)it.prods.size() + 1;
-    maxops = std::max(maxops, (int)it.prods.size() + 1);
+  for (int i = 0; i < n; ++i) {
+    W += (int64_t)items.nprod(i) + 1;
+    maxops = std::max(maxops, items.nprod(i) + 1);
   }
   if (W == 0) return pr;
   // rows are latency-bound: enough warps to bring a row to ~target_j
   // iterations, no more (idle warps issue nothing, partial ones waste FP64)
   const int best_w = (int)std::min<int64_t>(ntmax / 32, std::max<int64_t>(1, (W + 32 * target_j - 1) / (32 * target_j)));
   const int NB = 32 * best_w;
+  const int NW = (NB + 63) / 64;
   int J = (int)((W + NB - 1) / NB);
   struct Seg { int item, k, begin, len; bool split; };
   std::vector<Seg> segs;
-  std::vector<std::vector<int>> bins;
-  std::vector<int> nseg(items.size(), 1);
+  std::vector<int> order, lane, cnt, load;
+  std::vector<int> nseg(n, 1);
+  // room[t * NW ...]: bit b set while lane b holds at most t ops
+  std::vector<uint64_t> room;
   while (true) {
     if (maxops > J && J < 2) J = 2;
     segs.clear();
-    for (int i = 0; i < (int)items.size(); ++i) {
-      const int np = (int)items[i].prods.size();
+    for (int i = 0; i < n; ++i) {
+      const int np = items.nprod(i);
       if (np + 1 <= J) {
         nseg[i] = 1;
         segs.push_back({i, 0, 0, np, false});
@@ -588,48 +640,64 @@ DProg2 schedule2(std::vector<Item>& items, int ntmax, int target_j, std::vector<
         b += len;
       }
     }
-    std::vector<int> order(segs.size());
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return segs[x].len > segs[y].len; });
-    bins.assign(NB, {});
-    std::vector<int> load(NB, 0);
+    // longest first, stable: a counting sort (every length is below J)
+    cnt.assign((size_t)J + 1, 0);
+    for (const Seg& sg : segs) ++cnt[sg.len];
+    for (int l = J - 1, acc = 0; l >= 0; --l) {
+      const int c = cnt[l];
+      cnt[l] = acc;
+      acc += c;
+    }
+    order.resize(segs.size());
+    for (int si = 0; si < (int)segs.size(); ++si) order[cnt[segs[si].len]++] = si;
+    room.assign((size_t)J * NW, ~0ull);
+    if (NB & 63)
+      for (int t = 0; t < J; ++t) room[(size_t)t * NW + NW - 1] = (1ull << (NB & 63)) - 1;
+    load.assign(NB, 0);
+    lane.resize(order.size());
     bool ok = true;
-    int first_open = 0;
-    for (int si : order) {
-      const int len = segs[si].len + 1;
-      int b = first_open;
-      while (b < NB && load[b] + len > J) ++b;
-      if (b == NB) { ok = false; break; }
-      bins[b].push_back(si);
-      load[b] += len;
-      while (first_open < NB && load[first_open] == J) ++first_open;
+    for (size_t o = 0; o < order.size(); ++o) {
+      const int len = segs[order[o]].len + 1;
+      const int b = first_set(&room[(size_t)(J - len) * NW], NW);
+      if (b < 0) { ok = false; break; }
+      lane[o] = b;
+      const int l0 = load[b], l1 = l0 + len;
+      for (int t = l0; t < std::min(l1, J); ++t) room[(size_t)t * NW + (b >> 6)] &= ~(1ull << (b & 63));
+      load[b] = l1;
     }
     if (ok) break;
     ++J;
   }
+  // segments per lane in placement order (CSR)
+  std::vector<int> lane_off(NB + 1, 0), lane_seg(order.size());
+  for (int b : lane) ++lane_off[b + 1];
+  for (int b = 0; b < NB; ++b) lane_off[b + 1] += lane_off[b];
+  {
+    std::vector<int> cur(lane_off.begin(), lane_off.end() - 1);
+    for (size_t o = 0; o < order.size(); ++o) lane_seg[cur[lane[o]]++] = order[o];
+  }
   // partial slots of split items, contiguous per item
-  std::vector<int> slot0(items.size(), -1);
+  std::vector<int> slot0(n, -1);
   int nslot = 0;
-  for (int i = 0; i < (int)items.size(); ++i)
+  for (int i = 0; i < n; ++i)
     if (nseg[i] > 1) { slot0[i] = slot_base + nslot; nslot += nseg[i]; }
   if (slot_base + nslot >= 65535) throw Error(WG_ERANGE, "program exceeds 65535 partial slots");
   int used = 0;
-  for (int b = 0; b < NB; ++b) if (!bins[b].empty()) used = b + 1;
+  for (int b = 0; b < NB; ++b) if (lane_off[b + 1] > lane_off[b]) used = b + 1;
   const int nt = ((used + 31) / 32) * 32;
   pr.J = J;
   pr.nt = nt;
   pr.nslot = nslot;
   out.resize(out.size() + (size_t)J * nt, DEntry{pack_code(0, 0, 0, op::NOP), 0.0});
   DEntry* base = out.data() + pr.off;
-  for (int t = 0; t < nt; ++t) {
+  for (int t = 0; t < std::min(nt, NB); ++t) {
     int j = 0;
-    for (int si : bins[t]) {
-      const Seg& sg = segs[si];
-      const Item& it = items[sg.item];
-      for (int q = 0; q < sg.len; ++q, ++j) {
-        const Ent& e = it.prods[sg.begin + q];
-        base[(size_t)j * nt + t] = DEntry{pack_code(e.a, e.b, 0, op::PROD), e.p};
-      }
+    for (int x = lane_off[t]; x < lane_off[t + 1]; ++x) {
+      const Seg& sg = segs[lane_seg[x]];
+      const Item& it = items.items[sg.item];
+      const Ent* e = items.ents.data() + items.off[sg.item] + sg.begin;
+      for (int q = 0; q < sg.len; ++q, ++j)
+        base[(size_t)j * nt + t] = DEntry{pack_code(e[q].a, e[q].b, 0, op::PROD), e[q].p};
       if (sg.split)
         base[(size_t)j * nt + t] = DEntry{pack_code(0, 0, slot0[sg.item] + sg.k, op::FIN_PART), 0.0};
       else
@@ -639,10 +707,11 @@ DProg2 schedule2(std::vector<Item>& items, int ntmax, int target_j, std::vector<
   }
   // combine entries
   pr.comb = (int64_t)out.size();
-  for (int i = 0; i < (int)items.size(); ++i) {
+  for (int i = 0; i < n; ++i) {
     if (nseg[i] <= 1) continue;
+    const Item& it = items.items[i];
     const uint64_t sl = (uint64_t)(uint32_t)slot0[i] | ((uint64_t)(uint32_t)nseg[i] << 32);
-    out.push_back(DEntry{pack_code(items[i].c, items[i].fa, items[i].fb, items[i].fin), bits_to_double(sl)});
+    out.push_back(DEntry{pack_code(it.c, it.fa, it.fb, it.fin), bits_to_double(sl)});
     ++pr.ncomb;
   }
   return pr;
@@ -666,13 +735,25 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
   std::vector<FamInfo> info(NF);
   std::vector<std::vector<int>> lvl(NF);
   std::vector<std::array<double, 3>> cost(NF);
+  // per family and node: splits of its compatible non-leaf clades plus its
+  // compatible clades (the weight tasks are filled by)
+  std::vector<std::vector<double>> node_w(NF);
   for (int f = 0; f < NF; ++f)
     if (ccds[f]->n_clades >= 65535) throw Error(WG_ERANGE, "CCD with 65535 or more clades");
   parallel_for(NF, opt.threads, [&](size_t f) {
-    compat_of(m, *ccds[f], info[f], true);
+    const CCD& c = *ccds[f];
+    compat_of(m, c, info[f], true);
     double w;
-    family_cost(m, *ccds[f], info[f], cost[f][0], cost[f][1], cost[f][2], w);
-    lvl[f] = split_levels(*ccds[f]);
+    family_cost(m, c, info[f], cost[f][0], cost[f][1], cost[f][2], w);
+    lvl[f] = split_levels(c);
+    node_w[f].assign(K, 0.0);
+    for (int k = 0; k < K; ++k) {
+      const std::vector<int>& ix = info[f].idx[k];
+      double T = 0;
+      for (int g = 0; g < c.n_clades; ++g)
+        if (ix[g] >= 0 && c.nleaves[g] > 1) T += c.split_off[g + 1] - c.split_off[g];
+      node_w[f][k] = T + info[f].ncompat[k];
+    }
   });
   for (int f = 0; f < NF; ++f) {  // summed in family order
     P.flops_fwd += cost[f][0];
@@ -713,15 +794,8 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
     const int ka = m.ch0[k], kb = m.ch1[k];
     // families with compatible clades at k, heaviest first
     std::vector<std::pair<double, int>> fw;
-    for (int f = 0; f < NF; ++f) {
-      const int C = info[f].ncompat[k];
-      if (C == 0) continue;
-      const CCD& c = *ccds[f];
-      double T = 0;
-      for (int g = 0; g < c.n_clades; ++g)
-        if (info[f].idx[k][g] >= 0 && c.nleaves[g] > 1) T += c.split_off[g + 1] - c.split_off[g];
-      fw.emplace_back(T + C, f);
-    }
+    for (int f = 0; f < NF; ++f)
+      if (info[f].ncompat[k] > 0) fw.emplace_back(node_w[f][k], f);
     std::stable_sort(fw.begin(), fw.end(), [](auto& x, auto& y) { return x.first > y.first; });
     // next-fit into tasks
     std::vector<std::vector<int>> groups;
@@ -795,38 +869,32 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       // ---- forward programs
       const bool has_rows = kind != WG_NODE_ROOT && m.nrow[k] > 1;
       if (has_rows || (opt.adjoint && kind == WG_NODE_WGD)) {
-        std::vector<Item> items, titems;
+        ItemList items;
+        ScatterList titems(opt.adjoint ? R : 0);
         // row programs read both operand fields of every entry: finalize
         // entries carry their own clade in f0 and f1
-        if (opt.adjoint) {
-          titems.resize(R);
-          for (int x = 0; x < R; ++x) { titems[x].c = x; titems[x].fin = op::FIN_ADJ; titems[x].fa = x; titems[x].fb = x; }
-        }
+        for (int x = 0; x < (int)titems.items.size(); ++x) titems.items[x] = {x, op::FIN_ADJ, x, x};
         for (int i = 0; i < nf; ++i) {
           const CCD& c = *ccds[fams[i]];
           for (int g = 0; g < c.n_clades; ++g) {
             const int pg = pos(i, g);
             if (pg < 0) continue;
-            Item it;
-            it.c = pg;
-            it.fin = op::FIN_DUP;
-            it.fa = pg;
-            it.fb = pg;
+            items.open({pg, op::FIN_DUP, pg, pg});
             if (c.nleaves[g] > 1)
               for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s) {
                 const int a = pos(i, c.g1[s]), b = pos(i, c.g2[s]);
                 if (a < 0 || b < 0) throw Error(WG_EPARSE, "split operand incompatible with a compatible clade");
-                it.prods.push_back({a, b, c.p[s]});
+                items.prod(a, b, c.p[s]);
                 if (opt.adjoint) {
-                  titems[a].prods.push_back({pg, b, c.p[s]});
-                  titems[b].prods.push_back({pg, a, c.p[s]});
+                  titems.add(a, pg, b, c.p[s]);
+                  titems.add(b, pg, a, c.p[s]);
                 }
               }
-            items.push_back(std::move(it));
+            items.close();
           }
         }
         if (has_rows) T.dup = schedule2(items, NT, opt.target_j, entries);
-        if (opt.adjoint) T.tdup = schedule2(titems, NT, opt.target_j, entries);
+        if (opt.adjoint) T.tdup = schedule2(titems.finish(), NT, opt.target_j, entries);
       }
       if (kind == WG_NODE_LEAF) {
         std::vector<int> aux(R, 0);
@@ -840,35 +908,28 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
         T.aux = put_int(meta, aux);
       } else if (kind == WG_NODE_WGD) {
         if (T.wa != R) throw Error(WG_EINVAL, "WGD node and its child differ in compatible clades");
-        std::vector<Item> items;
+        ItemList items;
         for (int i = 0; i < nf; ++i) {
           const CCD& c = *ccds[fams[i]];
           for (int g = 0; g < c.n_clades; ++g) {
             const int pg = pos(i, g);
             if (pg < 0) continue;
-            Item it;
-            it.c = pg;
-            it.fin = op::FIN_WGD;
-            it.fa = posa(i, g);
+            items.open({pg, op::FIN_WGD, posa(i, g), 0xFFFF});
             if (c.nleaves[g] > 1)
               for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s)
-                it.prods.push_back({posa(i, c.g1[s]), posa(i, c.g2[s]), c.p[s]});
-            items.push_back(std::move(it));
+                items.prod(posa(i, c.g1[s]), posa(i, c.g2[s]), c.p[s]);
+            items.close();
           }
         }
         T.init = schedule2(items, NT, opt.target_j, entries);
       } else {
         // speciation + loss (internal) or Πspec + Πloss of the root row
-        std::vector<Item> items;
+        ItemList items;
         std::vector<std::array<int, 2>> loss(R, {-1, -1});
         std::vector<int> inva(T.wa, -1), invb(T.wb, -1);
-        std::vector<Item> ta, tb;
-        if (opt.adjoint) {
-          ta.resize(T.wa);
-          tb.resize(T.wb);
-          for (int x = 0; x < T.wa; ++x) { ta[x].c = x; ta[x].fin = op::FIN_TOP; }
-          for (int x = 0; x < T.wb; ++x) { tb[x].c = x; tb[x].fin = op::FIN_TOP; }
-        }
+        ScatterList ta(opt.adjoint ? T.wa : 0), tb(opt.adjoint ? T.wb : 0);
+        for (int x = 0; x < (int)ta.items.size(); ++x) ta.items[x] = {x, op::FIN_TOP, 0xFFFF, 0xFFFF};
+        for (int x = 0; x < (int)tb.items.size(); ++x) tb.items[x] = {x, op::FIN_TOP, 0xFFFF, 0xFFFF};
         for (int i = 0; i < nf; ++i) {
           const CCD& c = *ccds[fams[i]];
           for (int g = 0; g < c.n_clades; ++g) {
@@ -878,35 +939,31 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
             loss[pg] = {la, lb};
             if (la >= 0) inva[la] = pg;
             if (lb >= 0) invb[lb] = pg;
-            Item it;
-            it.c = pg;
-            it.fin = op::FIN_SPEC;
-            it.fa = la < 0 ? 0xFFFF : la;
-            it.fb = lb < 0 ? 0xFFFF : lb;
+            items.open({pg, op::FIN_SPEC, la < 0 ? 0xFFFF : la, lb < 0 ? 0xFFFF : lb});
             if (c.nleaves[g] > 1)
               for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s) {
                 const int g1 = c.g1[s], g2 = c.g2[s];
                 const int a1 = posa(i, g1), b2 = posb(i, g2), b1 = posb(i, g1), a2 = posa(i, g2);
                 if (a1 >= 0 && b2 >= 0) {
-                  it.prods.push_back({a1, b2, c.p[s]});
-                  if (opt.adjoint) { ta[a1].prods.push_back({pg, b2, c.p[s]}); tb[b2].prods.push_back({pg, a1, c.p[s]}); }
+                  items.prod(a1, b2, c.p[s]);
+                  if (opt.adjoint) { ta.add(a1, pg, b2, c.p[s]); tb.add(b2, pg, a1, c.p[s]); }
                 }
                 if (b1 >= 0 && a2 >= 0) {
-                  it.prods.push_back({a2, b1, c.p[s]});
-                  if (opt.adjoint) { ta[a2].prods.push_back({pg, b1, c.p[s]}); tb[b1].prods.push_back({pg, a2, c.p[s]}); }
+                  items.prod(a2, b1, c.p[s]);
+                  if (opt.adjoint) { ta.add(a2, pg, b1, c.p[s]); tb.add(b1, pg, a2, c.p[s]); }
                 }
               }
-            items.push_back(std::move(it));
+            items.close();
           }
         }
         T.init = schedule2(items, NT, opt.target_j, entries);
         T.loss = put_int2(meta, loss);
         if (opt.adjoint) {
-          for (int x = 0; x < T.wa; ++x) ta[x].fa = inva[x] < 0 ? 0xFFFF : inva[x];
-          for (int x = 0; x < T.wb; ++x) tb[x].fa = invb[x] < 0 ? 0xFFFF : invb[x];
-          T.ta = schedule2(ta, NT, opt.target_j, entries);
+          for (int x = 0; x < T.wa; ++x) ta.items[x].fa = inva[x] < 0 ? 0xFFFF : inva[x];
+          for (int x = 0; x < T.wb; ++x) tb.items[x].fa = invb[x] < 0 ? 0xFFFF : invb[x];
+          T.ta = schedule2(ta.finish(), NT, opt.target_j, entries);
           // the adjoint runs tb straight after ta: disjoint partial slots
-          T.tb = schedule2(tb, NT, opt.target_j, entries, T.ta.nslot);
+          T.tb = schedule2(tb.finish(), NT, opt.target_j, entries, T.ta.nslot);
           T.inva = put_int(meta, inva);
           T.invb = put_int(meta, invb);
         }
@@ -917,37 +974,38 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
         int nl = 0;
         for (int i = 0; i < nf; ++i)
           for (int v : lvl[fams[i]]) nl = std::max(nl, v + 1);
-        std::vector<std::vector<Item>> lw(nl), tlw(nl);
+        std::vector<ItemList> lw(nl), tlw(nl);
         std::vector<int> plevel(R, 0);
         for (int i = 0; i < nf; ++i) {
           const CCD& c = *ccds[fams[i]];
           for (int g = 0; g < c.n_clades; ++g) plevel[pos(i, g)] = lvl[fams[i]][g];
         }
-        std::vector<Item> tby;
-        if (opt.adjoint) {
-          tby.resize(R);
-          for (int x = 0; x < R; ++x) { tby[x].c = x; tby[x].fin = op::FIN_TLVL; tby[x].fa = x; tby[x].fb = x; }
-        }
+        ScatterList tby(opt.adjoint ? R : 0);
+        for (int x = 0; x < (int)tby.items.size(); ++x) tby.items[x] = {x, op::FIN_TLVL, x, x};
         for (int i = 0; i < nf; ++i) {
           const CCD& c = *ccds[fams[i]];
           for (int g = 0; g < c.n_clades; ++g) {
             const int pg = pos(i, g);
-            Item it;
-            it.c = pg;
-            it.fin = op::FIN_LVL;
-            it.fa = pg;
-            it.fb = pg;
+            ItemList& L = lw[plevel[pg]];
+            L.open({pg, op::FIN_LVL, pg, pg});
             if (c.nleaves[g] > 1)
               for (int s = c.split_off[g]; s < c.split_off[g + 1]; ++s) {
                 const int a = pos(i, c.g1[s]), b = pos(i, c.g2[s]);
-                it.prods.push_back({a, b, c.p[s]});
-                if (opt.adjoint) { tby[a].prods.push_back({pg, b, c.p[s]}); tby[b].prods.push_back({pg, a, c.p[s]}); }
+                L.prod(a, b, c.p[s]);
+                if (opt.adjoint) { tby.add(a, pg, b, c.p[s]); tby.add(b, pg, a, c.p[s]); }
               }
-            lw[plevel[pg]].push_back(std::move(it));
+            L.close();
           }
         }
-        if (opt.adjoint)
-          for (int x = 0; x < R; ++x) tlw[plevel[x]].push_back(std::move(tby[x]));
+        if (opt.adjoint) {
+          const ItemList t = tby.finish();
+          for (int x = 0; x < R; ++x) {
+            ItemList& L = tlw[plevel[x]];
+            L.open(t.items[x]);
+            L.ents.insert(L.ents.end(), t.ents.begin() + t.off[x], t.ents.begin() + t.off[x + 1]);
+            L.close();
+          }
+        }
         T.nlvl = nl;
         T.lvl = (int64_t)tb.progs.size();
         for (int L = 0; L < nl; ++L) tb.progs.push_back(schedule2(lw[L], NT, opt.target_j, entries));
