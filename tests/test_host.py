@@ -73,6 +73,32 @@ def test_ale_reader_matches_oracle(W, O, ex1_tree, ex1_files):
             assert a["nleaves"][i] == d["nleaves"] and a["counts"][i] == d["count"]
 
 
+def test_set_sampling_probabilities(W, O):
+    # test/runtests.jl:80-93: setsamplingp! gives every leaf its probability in
+    # getθ; beyond that, a leaf's first ε is its p (src/model.jl:170), so the
+    # slice tables and the condition follow the oracle given the same p
+    nw = W.nwstr(W.extree())
+    t = W.readnw(nw)
+    n = len(W.postwalk(t))
+    wm = W.WhaleModel(W.DLWGD(λ=np.ones(n), μ=np.ones(n), η=0.9), t, 0.05)
+    rng = np.random.default_rng(5)
+    d = {leaf.name: float(rng.random()) for leaf in W.getleaves(t)}
+    wm.setsamplingp(d)
+    p = wm.node_rates()[4]
+    leaves = [m for m in wm.order if m.kind == 0]
+    assert len(leaves) == len(d)
+    for m in leaves:
+        assert p[m.pos] == d[m.name]
+    om = O.OracleModel(nw, 0.05)
+    e, f, s = wm.tables()
+    oe, of, os_ = om.tables(np.ones(n), np.ones(n), eta=0.9, p=wm.rates.p)
+    assert np.array_equal(e, oe) and np.array_equal(f, of) and np.array_equal(s, os_)
+    assert wm.condition_value() == pytest.approx(om.condition(np.ones(n), np.ones(n), eta=0.9, p=wm.rates.p), rel=1e-14)
+    # a changed probability reaches the tables
+    wm.setsamplingp({**d, leaves[0].name: 0.5})
+    assert not np.array_equal(wm.tables()[0], e)
+
+
 def test_mul_tree_reader(W, O):
     nw = read(os.path.join(GOLDEN, "example5_tree.nw")).strip()
     t = W.readnw(nw)
