@@ -515,9 +515,11 @@ namespace {
 
 // A task built apart from the others: its programs' entries, int tables,
 // staging map and level programs with task-local offsets.
+using EntryBuf = std::vector<DEntry, UninitAlloc<DEntry>>;
+
 struct TaskBuild {
   DTask T;
-  std::vector<DEntry> entries;
+  EntryBuf entries;
   std::vector<int32_t> meta;
   std::vector<int64_t> gmap;
   std::vector<DProg2> progs;
@@ -596,7 +598,7 @@ inline int first_set(const uint64_t* w, int nw) {
 // room for them (first-fit decreasing into lanes of J ops); J grows until
 // they fit.  Partial slots are numbered from slot_base (a program run right
 // after another without a barrier takes slots after the other's).
-DProg2 schedule2(const ItemList& items, int ntmax, int target_j, std::vector<DEntry>& out, int slot_base = 0) {
+DProg2 schedule2(const ItemList& items, int ntmax, int target_j, EntryBuf& out, int slot_base = 0) {
   DProg2 pr;
   pr.off = (int64_t)out.size();
   const int n = items.size();
@@ -688,9 +690,11 @@ DProg2 schedule2(const ItemList& items, int ntmax, int target_j, std::vector<DEn
   pr.J = J;
   pr.nt = nt;
   pr.nslot = nslot;
-  out.resize(out.size() + (size_t)J * nt, DEntry{pack_code(0, 0, 0, op::NOP), 0.0});
+  // every position is written: a lane's segments, then NOPs to J
+  out.resize(out.size() + (size_t)J * nt);
   DEntry* base = out.data() + pr.off;
-  for (int t = 0; t < std::min(nt, NB); ++t) {
+  const DEntry nop{pack_code(0, 0, 0, op::NOP), 0.0};
+  for (int t = 0; t < nt; ++t) {
     int j = 0;
     for (int x = lane_off[t]; x < lane_off[t + 1]; ++x) {
       const Seg& sg = segs[lane_seg[x]];
@@ -704,6 +708,7 @@ DProg2 schedule2(const ItemList& items, int ntmax, int target_j, std::vector<DEn
         base[(size_t)j * nt + t] = DEntry{pack_code(it.c, it.fa, it.fb, it.fin), 0.0};
       ++j;
     }
+    for (; j < J; ++j) base[(size_t)j * nt + t] = nop;
   }
   // combine entries
   pr.comb = (int64_t)out.size();
@@ -784,7 +789,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
   P.level_smem_adj_h.assign(H + 1, 0);
   // gradient reduction contributions
   std::vector<std::vector<int64_t>> red(3 * (size_t)NR + K + 1);
-  std::vector<std::vector<DEntry>> entry_chunks;
+  std::vector<EntryBuf> entry_chunks;
   std::vector<int64_t> entry_off;
   int64_t n_entries = 0;
   auto eps_top_row = [&](int k) { return m.row_off[k] + m.nrow[k] - 1; };
@@ -829,7 +834,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
     auto build = [&](size_t gi, TaskBuild& tb) {
       const auto& fams = groups[gi];
       DTask& T = tb.T;
-      std::vector<DEntry>& entries = tb.entries;
+      EntryBuf& entries = tb.entries;
       std::vector<int32_t>& meta = tb.meta;
       const int nf = (int)fams.size();
       T.node = k;
@@ -1126,9 +1131,9 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
   }
   P.entries.resize((size_t)n_entries);
   parallel_for(entry_chunks.size(), opt.threads, [&](size_t i) {
-    std::vector<DEntry>& c = entry_chunks[i];
+    EntryBuf& c = entry_chunks[i];
     if (!c.empty()) std::memcpy(P.entries.data() + entry_off[i], c.data(), c.size() * sizeof(DEntry));
-    std::vector<DEntry>().swap(c);
+    EntryBuf().swap(c);
   });
   // heaviest tasks first inside each launch
   auto by_cost = [&](int a, int b) {
