@@ -43,7 +43,7 @@ NEIGHBOURS: Dict[str, Tuple[int, ...]] = {
 }
 _ENV = {"target_ops": "WG_PACK_TARGET_OPS", "target_j": "WG_PACK_TARGET_J", "root_group": "WG_PACK_ROOT_GROUP",
         "heavy_ops": "WG_PACK_HEAVY_OPS"}
-_env_lock = threading.Lock()
+_env_lock = threading.RLock()  # nested settings restore in order
 
 
 @contextlib.contextmanager
