@@ -175,8 +175,11 @@ CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& nam
   int64_t observations = -1;
   std::vector<int64_t> bip(cap + 1, 0);
   std::vector<char> has_bip(cap + 1, 0), has_dip(cap + 1, 0), has_set(cap + 1, 0);
-  std::vector<std::vector<std::array<int64_t, 3>>> dip(cap + 1);
-  std::vector<std::vector<int64_t>> set_id(cap + 1);
+  // Dip lines in file order (parent, γ1, γ2, count); grouped by parent below
+  std::vector<std::array<int64_t, 4>> diplines;
+  // set-id lines: the members of set k are pool[set_off[k] .. + set_len[k])
+  // (a repeated id: its last line)
+  std::vector<int64_t> pool, set_off(cap + 1, 0), set_len(cap + 1, 0);
   std::vector<std::string> leaf_id(leaf_lines + 1);  // leaf number -> gene name
   std::vector<char> has_leaf(leaf_lines + 1, 0);
   for (auto& l : leaves) leaf_id[l.first] = std::move(l.second), has_leaf[l.first] = 1;
@@ -207,13 +210,15 @@ CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& nam
         }
         case DIP: {
           if (v.size() < 4) throw Error(WG_EPARSE, "ALE: bad Dip_counts line");
-          if (v[0] >= 0 && v[0] <= cap) dip[v[0]].push_back({v[1], v[2], v[3]}), has_dip[v[0]] = 1;
+          if (v[0] >= 0 && v[0] <= cap) diplines.push_back({v[0], v[1], v[2], v[3]}), has_dip[v[0]] = 1;
           break;
         }
         case SETID: {
           const int64_t id = v[0];
           if (id < 1 || id >= cap) throw Error(WG_EPARSE, "ALE: set ids are not contiguous 1..n");
-          set_id[id].assign(v.begin() + 1, v.end());
+          set_off[id] = (int64_t)pool.size();
+          set_len[id] = (int64_t)v.size() - 1;
+          pool.insert(pool.end(), v.begin() + 1, v.end());
           has_set[id] = 1;
           break;
         }
@@ -229,24 +234,26 @@ CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& nam
   std::vector<int64_t> themap(leaf_lines + 1, -1);  // leaf id -> set id
   for (int64_t k = 1; k < cap; ++k) {
     if (!has_set[k]) continue;
-    auto& v = set_id[k];
-    if (v.size() == 1) {
+    int64_t* v = pool.data() + set_off[k];
+    const int64_t len = set_len[k];
+    if (len == 1) {
       const int64_t x = v[0];
       if (x < 0 || x > leaf_lines || !has_leaf[x]) throw Error(WG_EPARSE, "ALE: leaf id without a name");
       bip[k] = observations, has_bip[k] = 1;
-      dip[k].clear(), has_dip[k] = 1;
+      has_dip[k] = 1;  // leaf sets have no splits
       leafname[k] = leaf_id[x];
       is_leafset[k] = 1;
       themap[x] = k;
     } else {
-      for (auto& x : v) {
+      for (int64_t i = 0; i < len; ++i) {
+        int64_t& x = v[i];
         if (x < 0 || x > leaf_lines || themap[x] < 0) throw Error(WG_EPARSE, "ALE: set refers to an unknown leaf");
         x = themap[x];
       }
     }
   }
   for (int64_t x = 0; x <= leaf_lines; ++x)
-    if (themap[x] >= 0) set_id[themap[x]] = {themap[x]};
+    if (themap[x] >= 0) pool[set_off[themap[x]]] = themap[x];
   // addubiquitous!
   int64_t nset = 0, kmin = -1, kmax = -1;
   for (int64_t k = 1; k < cap; ++k)
@@ -276,7 +283,8 @@ CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& nam
   byset.reserve((size_t)G);
   for (int64_t k = 1; k < G; ++k) {
     uint64_t* b = bits.data() + (size_t)k * W;
-    for (int64_t x : set_id[k]) {
+    for (int64_t i = 0; i < set_len[k]; ++i) {
+      const int64_t x = pool[set_off[k] + i];
       if (x < 1 || x >= G || leafbit[x] < 0) throw Error(WG_EPARSE, "ALE: set refers to a non-leaf set");
       b[leafbit[x] >> 6] |= 1ull << (leafbit[x] & 63);
     }
@@ -306,19 +314,36 @@ CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& nam
     rootsplits.push_back({i, j, bip[j]});
   }
   if (rootsplits.empty()) throw Error(WG_EPARSE, "ALE: no complementary clade pairs for the root");
-  dip[G] = rootsplits, has_dip[G] = 1;
+  has_dip[G] = 1;  // its splits: rootsplits (Dip lines of G are not read)
   bip[G] = N, has_bip[G] = 1;
   {
-    std::vector<int64_t> u = set_id[rootsplits.back()[0]];
-    const auto& v = set_id[rootsplits.back()[1]];
-    u.insert(u.end(), v.begin(), v.end());
+    const int64_t i = rootsplits.back()[0], j = rootsplits.back()[1];
+    std::vector<int64_t> u(pool.begin() + set_off[i], pool.begin() + set_off[i] + set_len[i]);
+    u.insert(u.end(), pool.begin() + set_off[j], pool.begin() + set_off[j] + set_len[j]);
     std::sort(u.begin(), u.end());
-    set_id[G] = u;
+    set_off[G] = (int64_t)pool.size();
+    set_len[G] = (int64_t)u.size();
+    pool.insert(pool.end(), u.begin(), u.end());
   }
+  // Dip lines grouped by parent, in file order within a parent
+  std::vector<int64_t> dip_off(cap + 2, 0);
+  for (const auto& d : diplines) ++dip_off[d[0] + 1];
+  for (int64_t k = 0; k <= cap; ++k) dip_off[k + 1] += dip_off[k];
+  std::vector<std::array<int64_t, 3>> dipv(diplines.size());
+  {
+    std::vector<int64_t> cur(dip_off.begin(), dip_off.end() - 1);
+    for (const auto& d : diplines) dipv[cur[d[0]]++] = {d[1], d[2], d[3]};
+  }
+  // splits of set k: none for leaf sets, the complementary pairs for G
+  auto splits = [&](int64_t k) -> std::pair<const std::array<int64_t, 3>*, size_t> {
+    if (k == G) return {rootsplits.data(), rootsplits.size()};
+    if (is_leafset[k]) return {nullptr, 0};
+    return {dipv.data() + dip_off[k], (size_t)(dip_off[k + 1] - dip_off[k])};
+  };
   // CCD(ale, wm, spmap): order by (size, key)
   std::vector<std::pair<size_t, int64_t>> ord;
   ord.reserve((size_t)G);
-  for (int64_t k = 1; k <= G; ++k) ord.emplace_back(set_id[k].size(), k);
+  for (int64_t k = 1; k <= G; ++k) ord.emplace_back((size_t)set_len[k], k);
   std::sort(ord.begin(), ord.end());
   std::vector<int> idmap(cap + 1, -1);
   for (size_t i = 0; i < ord.size(); ++i) idmap[ord[i].second] = (int)i;
@@ -340,7 +365,7 @@ CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& nam
   cc->n_genes = (int)n;
   {
     size_t nsplit = 0;
-    for (auto& o : ord) nsplit += dip[o.second].size();
+    for (auto& o : ord) nsplit += splits(o.second).second;
     cc->g1.reserve(nsplit), cc->g2.reserve(nsplit), cc->p.reserve(nsplit);
     for (auto* v : {&cc->nleaves, &cc->split_off, &cc->sp_off}) v->reserve(ord.size() + 1);
     cc->counts.reserve(ord.size());
@@ -350,14 +375,23 @@ CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& nam
   cc->sp_off.push_back(0);
   cc->split_off.push_back(0);
   std::vector<int> sp;
+  // a clade's species, deduplicated by stamping (then sorted: few distinct)
+  int max_sp = 0;
+  for (int id : ids) {
+    if (id < 0) throw Error(WG_EINVAL, "negative species id");
+    max_sp = std::max(max_sp, id);
+  }
+  std::vector<int64_t> stamp((size_t)max_sp + 1, -1);
   for (size_t i = 0; i < ord.size(); ++i) {
     const int64_t k = ord[i].second;
     if (!has_bip[k]) throw Error(WG_EPARSE, "ALE: clade without a Bip count");
     cc->nleaves.push_back((int)ord[i].first);
-    cc->leaf_name.push_back(ord[i].first == 1 ? leafname[set_id[k][0]] : std::string());
+    cc->leaf_name.push_back(ord[i].first == 1 ? leafname[pool[set_off[k]]] : std::string());
     cc->counts.push_back(bip[k]);
     if (!has_dip[k] && ord[i].first > 1) throw Error(WG_EPARSE, "ALE: clade without Dip counts");
-    for (auto& t : dip[k]) {
+    const auto sk = splits(k);
+    for (size_t q = 0; q < sk.second; ++q) {
+      const auto& t = sk.first[q];
       const int a = t[0] >= 0 && t[0] <= cap ? idmap[t[0]] : -1, b = t[1] >= 0 && t[1] <= cap ? idmap[t[1]] : -1;
       if (a < 0 || b < 0) throw Error(WG_EPARSE, "ALE: split refers to an unknown set");
       cc->g1.push_back(a);
@@ -366,9 +400,11 @@ CCD* parse_ale(const char* text, size_t len, const std::vector<std::string>& nam
     }
     cc->split_off.push_back((int)cc->g1.size());
     sp.clear();
-    for (int64_t x : set_id[k]) sp.push_back(leafsp[x]);
+    for (int64_t q = 0; q < set_len[k]; ++q) {
+      const int s = leafsp[pool[set_off[k] + q]];
+      if (stamp[s] != k) stamp[s] = k, sp.push_back(s);
+    }
     std::sort(sp.begin(), sp.end());
-    sp.erase(std::unique(sp.begin(), sp.end()), sp.end());
     cc->sp.insert(cc->sp.end(), sp.begin(), sp.end());
     cc->sp_off.push_back((int)cc->sp.size());
   }
