@@ -513,15 +513,14 @@ namespace wg {
 
 namespace {
 
-// A task built apart from the others: its programs' entries, int tables,
-// staging map and level programs with task-local offsets.
+// A task built apart from the others: its programs' entries, int tables
+// and level programs with task-local offsets.
 using EntryBuf = std::vector<DEntry, UninitAlloc<DEntry>>;
 
 struct TaskBuild {
   DTask T;
   EntryBuf entries;
   std::vector<int32_t> meta;
-  std::vector<int64_t> gmap;
   std::vector<DProg2> progs;
   std::vector<int> col;  // first row position of each family of the group
   int smem_adj = 0, NT = 0;
@@ -794,17 +793,18 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
   int64_t n_entries = 0;
   auto eps_top_row = [&](int k) { return m.row_off[k] + m.nrow[k] - 1; };
 
+  // every node's families in task groups: compatible families, heaviest
+  // first, next-fit
+  std::vector<std::vector<std::vector<int>>> groups_of(K);
+  std::vector<std::vector<double>> ops_of(K);
   for (int k = 0; k < K; ++k) {
     const int kind = m.kind[k];
-    const int ka = m.ch0[k], kb = m.ch1[k];
-    // families with compatible clades at k, heaviest first
     std::vector<std::pair<double, int>> fw;
     for (int f = 0; f < NF; ++f)
       if (info[f].ncompat[k] > 0) fw.emplace_back(node_w[f][k], f);
     std::stable_sort(fw.begin(), fw.end(), [](auto& x, auto& y) { return x.first > y.first; });
-    // next-fit into tasks
-    std::vector<std::vector<int>> groups;
-    std::vector<double> group_ops;
+    std::vector<std::vector<int>>& groups = groups_of[k];
+    std::vector<double>& group_ops = ops_of[k];
     {
       // the root row is a chain of short same-row levels, so a root task
       // takes many more families for the same per-level work
@@ -829,17 +829,21 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       }
       if (!cur.empty()) { groups.push_back(cur); group_ops.push_back(ops); }
     }
-    // one task per group, built in parallel into task-local buffers and
-    // merged in group order (global offsets assigned there)
-    auto build = [&](size_t gi, TaskBuild& tb) {
-      const auto& fams = groups[gi];
+  }
+  // one task per group, all nodes' tasks built in one parallel pass (largest
+  // first) into task-local buffers; merged after, in node and group order
+  // (global offsets and the staging maps of the children's tops set there)
+  auto build = [&](int k, size_t gi, TaskBuild& tb) {
+      const int kind = m.kind[k];
+      const int ka = m.ch0[k], kb = m.ch1[k];
+      const auto& fams = groups_of[k][gi];
       DTask& T = tb.T;
       EntryBuf& entries = tb.entries;
       std::vector<int32_t>& meta = tb.meta;
       const int nf = (int)fams.size();
       T.node = k;
       T.nfam = nf;
-      const double gops = group_ops[gi];
+      const double gops = ops_of[k][gi];
       std::vector<int> col(nf + 1, 0), cola(nf + 1, 0), colb(nf + 1, 0);
       for (int i = 0; i < nf; ++i) {
         col[i + 1] = col[i] + info[fams[i]].ncompat[k];
@@ -862,15 +866,6 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       auto posa = [&](int i, int g) { const int j = info[fams[i]].idx[ka][g]; return j < 0 ? -1 : cola[i] + j; };
       auto posb = [&](int i, int g) { const int j = info[fams[i]].idx[kb][g]; return j < 0 ? -1 : colb[i] + j; };
       tb.col = col;
-      // staging maps of the children's top rows
-      for (int ch : {ka, kb}) {  // children's tops are final: their nodes came first
-        if (ch < 0) continue;
-        for (int i = 0; i < nf; ++i) {
-          const int C = info[fams[i]].ncompat[ch];
-          const int64_t src = toploc[(size_t)fams[i] * K + ch];
-          for (int j = 0; j < C; ++j) tb.gmap.push_back(src + j);
-        }
-      }
       // ---- forward programs
       const bool has_rows = kind != WG_NODE_ROOT && m.nrow[k] > 1;
       if (has_rows || (opt.adjoint && kind == WG_NODE_WGD)) {
@@ -1039,13 +1034,35 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       const int smem_adj = 6 * W2 + slots + 2 * m.nrow[k] + 16 * (NT / 32) + 32;
       tb.smem_adj = smem_adj;
       tb.NT = NT;
-    };
-    std::vector<TaskBuild> builds(groups.size());
-    parallel_for(groups.size(), opt.threads, [&](size_t gi) { build(gi, builds[gi]); });
-    for (size_t gi = 0; gi < groups.size(); ++gi) {
-      TaskBuild& tb = builds[gi];
+  };
+  std::vector<std::vector<TaskBuild>> builds(K);
+  std::vector<std::vector<std::exception_ptr>> errs(K);
+  std::vector<std::pair<int, int>> jobs;
+  for (int k = 0; k < K; ++k) {
+    builds[k].resize(groups_of[k].size());
+    errs[k].resize(groups_of[k].size());
+    for (int gi = 0; gi < (int)groups_of[k].size(); ++gi) jobs.emplace_back(k, gi);
+  }
+  std::stable_sort(jobs.begin(), jobs.end(),
+                   [&](auto& x, auto& y) { return ops_of[x.first][x.second] > ops_of[y.first][y.second]; });
+  parallel_for(jobs.size(), opt.threads, [&](size_t j) {
+    const auto [k, gi] = jobs[j];
+    try {
+      build(k, gi, builds[k][gi]);
+    } catch (...) {
+      errs[k][gi] = std::current_exception();
+    }
+  });
+  for (auto& ek : errs)  // the first failing task in node and group order
+    for (auto& e : ek)
+      if (e) std::rethrow_exception(e);
+  for (int k = 0; k < K; ++k) {
+    const int kind = m.kind[k];
+    const int ka = m.ch0[k], kb = m.ch1[k];
+    for (size_t gi = 0; gi < groups_of[k].size(); ++gi) {
+      TaskBuild& tb = builds[k][gi];
       DTask T = tb.T;
-      const auto& fams = groups[gi];
+      const auto& fams = groups_of[k][gi];
       const int nf = (int)fams.size();
       const int R = T.width, NT = tb.NT, smem_adj = tb.smem_adj;
       T.top = P.tops_doubles;
@@ -1062,8 +1079,16 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
         P.fam_col[fk] = tb.col[i];
         P.fam_ncol[fk] = info[fams[i]].ncompat[k];
       }
+      // staging maps of the children's top rows (final: their nodes came first)
       T.gmap = (int64_t)P.gmap.size();
-      P.gmap.insert(P.gmap.end(), tb.gmap.begin(), tb.gmap.end());
+      for (int ch : {ka, kb}) {
+        if (ch < 0) continue;
+        for (int i = 0; i < nf; ++i) {
+          const int C = info[fams[i]].ncompat[ch];
+          const int64_t src = toploc[(size_t)fams[i] * K + ch];
+          for (int j = 0; j < C; ++j) P.gmap.push_back(src + j);
+        }
+      }
       // entries, level programs and int tables: task-local offsets made global
       // (entries are copied once, in parallel, after the last node)
       const int64_t eb = n_entries;
@@ -1128,6 +1153,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       }
       P.tasks.push_back(T);
     }
+    std::vector<TaskBuild>().swap(builds[k]);
   }
   P.entries.resize((size_t)n_entries);
   parallel_for(entry_chunks.size(), opt.threads, [&](size_t i) {
