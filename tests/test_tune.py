@@ -42,6 +42,15 @@ def test_knobs_reach_the_packer(W):
     assert np.array_equal(_tasks(W, wm, ccds), base)  # the environment is restored
 
 
+def test_malformed_knob_is_refused(W, monkeypatch):
+    from whale_gb300 import synth
+
+    wl = synth.config0(n_families=4)
+    monkeypatch.setenv("WG_PACK_TARGET_OPS", "480x")
+    with pytest.raises(W.WhaleError, match="not an integer"):
+        _tasks(W, wl.model, wl.ccds())
+
+
 def test_descent_finds_the_optimum_of_a_known_cost(W):
     from whale_gb300 import autotune as tune
 

@@ -48,7 +48,9 @@ _env_lock = threading.RLock()  # nested settings restore in order
 
 @contextlib.contextmanager
 def packing(setting: Dict[str, int]):
-    """Batches created inside use the given packer knobs."""
+    """Batches created inside use the given packer knobs.  The knobs are
+    process-wide environment variables: a batch another thread creates
+    meanwhile packs with them too."""
     with _env_lock:
         old = {k: os.environ.get(v) for k, v in _ENV.items()}
         try:

@@ -39,7 +39,9 @@ inline int default_host_threads() {
 inline int64_t pack_knob(const char* name, int64_t dflt, int64_t lo, int64_t hi) {
   const char* e = std::getenv(name);
   if (!e || !*e) return dflt;
-  const long long v = std::atoll(e);
+  char* end = nullptr;
+  const long long v = std::strtoll(e, &end, 10);
+  if (end == e || *end != '\0') throw Error(WG_EINVAL, std::string(name) + " is not an integer");
   if (v < lo || v > hi) throw Error(WG_EINVAL, std::string(name) + " out of range");
   return (int64_t)v;
 }
