@@ -207,6 +207,16 @@ int wg_logpdf_plain(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, d
 int wg_logpdf_tables(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t family, double* out, int64_t cap,
                      int64_t* needed, double* logl);
 
+/* The DP tables of family i as the batch's last fetched evaluation left them
+ * (wg_logpdf, wg_logpdf_grad[_weighted], wg_fetch, wg_logpdf_tables), in the
+ * wg_logpdf_tables layout, and its log L; no evaluation here.  One batched
+ * logpdf! then one download per family: the order src/track.jl:18-21 names
+ * as the faster one for TreeTracker.  The batch must have WG_BATCH_TABLES;
+ * WG_ESTATE when no fetched evaluation holds the tables (none yet, one
+ * pending, or wg_logpdf_noalloc since).  *needed as wg_logpdf_tables. */
+int wg_batch_tables(wg_ctx* ctx, wg_batch* b, int32_t family, double* out, int64_t cap, int64_t* needed,
+                    double* logl);
+
 /* Forward evaluation that allocates nothing (no counterpart in the reference).
  * For callers that cannot allocate device memory when they evaluate: hosts
  * whose device memory is owned by another allocator or pool, and sampler

@@ -73,3 +73,56 @@ def test_host_backtracking_from_oracle_tables(W, O):
     for key, pr in (("duplication", dup / total), ("speciation", spe / total), ("sploss", los / total)):
         se = np.sqrt(max(pr * (1 - pr), 1e-4) / len(trees))
         assert abs(cnt[key] / len(trees) - pr) <= 4 * se
+
+
+def test_track_from_oracle_tables(W, O):
+    # TreeTracker (src/track.jl:11-82) with the oracle's tables standing in for
+    # the device: picks, seeds and summaries (src/rectree.jl:123-143)
+    from whale_gb300 import synth
+    from whale_gb300.track import _draw_seed, backtrack_tables, sumtrees, track_tables
+
+    wl = synth.config0(seed=8, n_families=6)
+    wm = wl.model
+    ccds = wl.ccds()[:3]
+    om = O.OracleModel(W.nwstr(wm.tree), wm.Δt)
+    ocs = [O.OracleCCD(om, t) for t in wl.ale[:3]]
+    r = wm.rates
+
+    def tables_of(m, f):
+        x = m.rates
+        return om.family_tables(ocs[f], [x.λ], [x.μ], q=x.q, eta=x.η, kind="ConstantDLWGD")
+
+    # one draw: every pick is it, and tree j of family f is the tree sampled
+    # directly from its tables with that pick's seed
+    trees = track_tables(tables_of, wm, ccds, [r], 6, seed=3, summary=False)
+    for f, c in enumerate(ccds):
+        assert len(trees[f]) == 6
+        for j in range(6):
+            ref = backtrack_tables(wm, c, tables_of(wm, f), n=1, seed=_draw_seed(3, j, f))[0]
+            assert trees[f][j].newick == ref.newick
+        genes = _genes(wl.ale[f])
+        for t in trees[f]:
+            assert sorted(n.name for n in t.root.postwalk() if n.isleaf() and n.label != "loss") == genes
+    again = track_tables(tables_of, wm, ccds, [r], 6, seed=3, summary=False)
+    assert [[t.newick for t in x] for x in again] == [[t.newick for t in x] for x in trees]
+    # two draws (the second with ten times the duplication rate): both are used
+    hi = r(dict(λ=r.λ * 10))
+    sums = track_tables(tables_of, wm, ccds, [r, hi], 40, seed=4)
+    raw = track_tables(tables_of, wm, ccds, [r, hi], 40, seed=4, summary=False)
+    for s, t, c in zip(sums, raw, ccds):
+        freqs = [fr for fr, _ in s.trees]
+        assert abs(sum(freqs) - 1) < 1e-12 and freqs == sorted(freqs, reverse=True)
+        assert all(0 < x <= 1 for cr in s.credibility for x in cr)
+        # expected event counts = mean over the samples of each tree's counts
+        K = len(wm.order)
+        mean = {lab: np.zeros(K) for lab in s.events}
+        for tr in t:
+            for n in tr.root.postwalk():
+                mean[n.label][n.node] += 1 / len(t)
+        for lab in s.events:
+            assert np.allclose(s.events[lab], mean[lab], atol=1e-12)
+        s2 = sumtrees(t, c, wm)  # the summary of the same draws
+        assert [(fr, tr.newick) for fr, tr in s2.trees] == [(fr, tr.newick) for fr, tr in s.trees]
+    dup = sum(s.events["duplication"].sum() for s in sums)
+    dup_lo = sum(s.events["duplication"].sum() for s in track_tables(tables_of, wm, ccds, [r], 40, seed=4))
+    assert dup > dup_lo

@@ -113,3 +113,41 @@ def test_root_event_frequencies_follow_the_dp(W, O, fam):
     for key, pr in (("duplication", dup / total), ("speciation", spe / total), ("sploss", los / total)):
         se = np.sqrt(max(pr * (1 - pr), 1e-4) / n)
         assert abs(cnt[key] / n - pr) <= 4 * se
+
+
+def test_track_matches_per_family_backtracking(W, fam):
+    # TreeTracker on the device (src/track.jl:11-82): one batched logpdf! per
+    # pick, each family's tables downloaded without re-evaluating
+    # (wg_batch_tables) and sampled; every tree equals wg_backtrack's on the
+    # same layout, draw and seed
+    import ctypes as C
+
+    from whale_gb300 import _native as N
+    from whale_gb300.track import _draw_seed
+
+    wl, wm, ccds = fam
+    r = wm.rates
+    draws = [r, r(dict(λ=r.λ * 3, μ=r.μ * 0.5))]
+    trees = W.track(wm, ccds, draws, 5, seed=21, summary=False)
+    picks = np.random.default_rng(21).integers(len(draws), size=5)
+    b = W.Batch(wm, ccds, tables=True)
+    with pytest.raises(W.WhaleError, match="evaluate it first"):
+        b.last_tables(0)
+    L = N.lib()
+    for j, i in enumerate(picks):
+        m = wm(draws[i])
+        m.load()
+        for f in range(len(ccds)):
+            seed = C.c_uint64(_draw_seed(21, j, f))
+            need = N.i64()
+            N.check(L.wg_backtrack(b.ctx.h, m._struct.h, b.h, f, 1, seed, None, 0, C.byref(need)))
+            buf = C.create_string_buffer(need.value)
+            N.check(L.wg_backtrack(b.ctx.h, m._struct.h, b.h, f, 1, seed, buf, need.value, C.byref(need)))
+            ref = [ln for ln in buf.value.decode().split("\n") if ln]
+            assert [trees[f][j].newick] == ref
+    # after an evaluation the download equals logpdf!'s own tables
+    ll, tab = b.family_tables(wm, 2)
+    ll2, tab2 = b.last_tables(2)
+    assert ll2 == ll and np.array_equal(tab2, tab)
+    s = W.track(wm, ccds[:2], draws, 30, seed=2)
+    assert all(abs(sum(fr for fr, _ in x.trees) - 1) < 1e-12 for x in s)

@@ -180,6 +180,17 @@ class Batch:
                                          N.C.byref(need), N.C.byref(ll)))
         return ll.value, out[: need.value]
 
+    def last_tables(self, i: int):
+        """Family i's log L and DP tables as the last fetched evaluation of
+        this batch left them (no evaluation here; ``family_tables`` layout)."""
+        need = N.i64()
+        N.check(N.lib().wg_batch_tables(self.ctx.h, self.h, i, None, 0, N.C.byref(need), None))
+        out = np.zeros(max(need.value, 1))
+        ll = N.dbl()
+        N.check(N.lib().wg_batch_tables(self.ctx.h, self.h, i, N.dptr(out), need.value, N.C.byref(need),
+                                        N.C.byref(ll)))
+        return ll.value, out[: need.value]
+
 
 # cache of device batches keyed by the model structure and the CCD objects
 _batches: Dict[Tuple, Batch] = {}

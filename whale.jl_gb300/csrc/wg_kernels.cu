@@ -1402,6 +1402,7 @@ struct wg_batch {
   double* h_gred = nullptr;  // P per sub-batch
   bool grad_pending = false;
   bool pending = false;  // an enqueued evaluation has not been fetched yet
+  bool tables_fresh = false;  // d_tabs and h_logl hold the last fetched evaluation (WG_BATCH_TABLES)
   int launches[2] = {0, 0};  // kernels per recorded sequence: [forward only, with gradient]
   std::vector<wg_ccd*> ccds;  // not owned; for the lazily built plain layout
   std::unique_ptr<PlainBatch> plain;
@@ -1873,6 +1874,7 @@ void enqueue(wg_batch* b, const wg_model* m, bool grad, const double* weights = 
     if (!e) ck(cudaEventCreate(&e), "cudaEventCreate");
   // the pinned parameter buffer is read by the previous launch's copy
   if (b->pending) ck(cudaStreamSynchronize(ctx->stream), "pending evaluation");
+  b->tables_fresh = false;
   stage_params(b, m);
   const bool weighted = weights != nullptr;
   if (weighted) {
@@ -2013,6 +2015,7 @@ void fetch(wg_batch* b, const wg_model* m, double* per_family, double* total, do
   const bool grad = b->grad_pending;
   ck(cudaStreamSynchronize(s), "evaluation");  // the graph ends with the result downloads
   b->pending = false;
+  b->tables_fresh = (b->flags & WG_BATCH_TABLES) != 0;
   finish_timing(b->ctx);
   std::vector<double> gred;
   if (grad) {  // size classes summed in class order
@@ -2279,6 +2282,40 @@ int wg_logpdf_tables(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t family, doub
   });
 }
 
+int wg_batch_tables(wg_ctx* ctx, wg_batch* b, int32_t family, double* out, int64_t cap, int64_t* needed,
+                    double* logl) {
+  WG_GUARD({
+    if (!ctx || !b || b->ctx != ctx) throw Error(WG_EINVAL, "wg_batch_tables: bad arguments");
+    if (family < 0 || family >= b->NF) throw Error(WG_EINVAL, "family index out of range");
+    if (!(b->flags & WG_BATCH_TABLES)) throw Error(WG_ESTATE, "batch was created without WG_BATCH_TABLES");
+    const int K = b->K;
+    const SubBatch* sb = b->subs[b->fam_sub[family]].get();
+    const size_t lf = (size_t)b->fam_local[family];
+    int64_t need = 0;
+    for (int k = 0; k < K; ++k) need += (int64_t)b->nrow[k] * sb->fam_ncol[lf * K + k];
+    if (needed) *needed = need;
+    if (!out) return WG_OK;
+    if (cap < need) throw Error(WG_ERANGE, "output buffer too small");
+    if (b->pending || !b->tables_fresh)
+      throw Error(WG_ESTATE, "no fetched evaluation of this batch holds its tables (evaluate it first)");
+    ck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (logl) *logl = b->h_logl[family];
+    cudaStream_t s = ctx->stream;
+    int64_t o = 0;
+    for (int k = 0; k < K; ++k) {
+      const size_t fk = lf * K + k;
+      const int nc = sb->fam_ncol[fk];
+      if (nc > 0)
+        ck(cudaMemcpy2DAsync(out + o, nc * sizeof(double), sb->d_tabs + sb->fam_tab[fk] + sb->fam_col[fk],
+                             (size_t)sb->fam_w[fk] * sizeof(double), nc * sizeof(double), b->nrow[k],
+                             cudaMemcpyDeviceToHost, s),
+           "table download");
+      o += (int64_t)b->nrow[k] * nc;
+    }
+    ck(cudaStreamSynchronize(s), "table download");
+  });
+}
+
 int wg_backtrack(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t family, int32_t n_samples, uint64_t seed, char* out,
                  int64_t cap, int64_t* needed) {
   WG_GUARD({
@@ -2364,6 +2401,7 @@ extern "C" int wg_logpdf_noalloc(wg_ctx* ctx, wg_model* m, wg_batch* b, double* 
     double* scratch = noalloc_scratch(ctx->device);
     cudaStream_t s = ctx->stream;
     if (b->pending) ck(cudaStreamSynchronize(s), "pending evaluation");
+    b->tables_fresh = false;  // writes no tables; h_logl becomes this call's
     stage_params(b, m);
     ck(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(double) * (b->P + 2), cudaMemcpyHostToDevice, s),
        "params upload");

@@ -126,3 +126,136 @@ def backtrack(wm: WhaleModel, x: Union[CCD, Sequence[CCD]], n: int = 1, seed: in
                            C.byref(need)))
     lines = [ln for ln in buf.value.decode().split("\n") if ln]
     return [RecTree(ln, _parse(ln, wm)) for ln in lines]
+
+
+# ---- TreeTracker (src/track.jl:11-82) and tree summaries (src/rectree.jl) ----
+
+LABELS = ("loss", "wgd", "wgdloss", "duplication", "sploss", "speciation")  # src/track.jl:468
+
+
+@dataclass
+class TrackSummary:
+    """``RecSummary`` (src/rectree.jl:4-8) of one family's sampled trees.
+
+    trees: the distinct reconciled trees, most frequent first, as
+    (frequency, RecTree); credibility: for each of them, per node in
+    postorder, the fraction of all samples holding that node (the
+    reference's ``cred``); events: per label (LABELS), the expected number of
+    such events on every species node (``wm.order`` positions), i.e. the
+    frequency-weighted event counts of the distinct trees (the mean over the
+    samples); counts: the same counts per distinct tree."""
+    fname: str
+    trees: List[tuple]
+    credibility: List[List[float]]
+    events: dict
+    counts: List[dict]
+
+
+def _node_key(n: RecNode, sister: Optional[RecNode]):
+    # src/track.jl:111-113: a loss is its branch and its sister's clade; any
+    # other node its clade, branch and its children's (clade, branch) pairs
+    if n.label == "loss":
+        return (-1, n.node, sister.clade if sister is not None else -2)
+    return (n.clade, n.node, frozenset((c.clade, c.node) for c in n.children))
+
+
+def _node_keys(root: RecNode):
+    out = []
+
+    def walk(n: RecNode, sister: Optional[RecNode]):
+        for i, c in enumerate(n.children):
+            s = n.children[1 - i] if len(n.children) == 2 else None
+            walk(c, s)
+        out.append(_node_key(n, sister))
+
+    walk(root, None)
+    return out
+
+
+def sumtrees(trees: Sequence[RecTree], ccd: CCD, wm: WhaleModel) -> TrackSummary:
+    """``sumtrees`` (src/rectree.jl:123-143): distinct trees (by the set of
+    their node keys, as ``nodehash``), their frequencies, node credibilities
+    and event counts per species node."""
+    import numpy as np
+
+    n = len(trees)
+    if n == 0:
+        raise ValueError("no trees to summarise")
+    keys = [_node_keys(t.root) for t in trees]
+    tkeys = [frozenset(k) for k in keys]
+    clade_count = {}
+    for k in keys:
+        for x in k:
+            clade_count[x] = clade_count.get(x, 0) + 1
+    first, count = {}, {}
+    for i, tk in enumerate(tkeys):
+        first.setdefault(tk, i)
+        count[tk] = count.get(tk, 0) + 1
+    order = sorted(count, key=lambda tk: (-count[tk], first[tk]))
+    K = len(wm.order)
+    events = {lab: np.zeros(K) for lab in LABELS}
+    out_trees, cred, counts = [], [], []
+    for tk in order:
+        t = trees[first[tk]]
+        f = count[tk] / n
+        c = {lab: np.zeros(K, dtype=np.int64) for lab in LABELS}
+        for node in t.root.postwalk():
+            if node.label in c and 0 <= node.node < K:
+                c[node.label][node.node] += 1
+        for lab in LABELS:
+            events[lab] += f * c[lab]
+        out_trees.append((f, t))
+        cred.append([clade_count[x] / n for x in keys[first[tk]]])
+        counts.append(c)
+    return TrackSummary(getattr(ccd, "fname", ""), out_trees, cred, events, counts)
+
+
+def _draw_seed(seed: int, j: int, f: int) -> int:
+    return (seed * 0x9E3779B97F4A7C15 + j * 0xBF58476D1CE4E5B9 + f * 0x94D049BB133111EB + 1) % (1 << 64)
+
+
+def track_tables(tables_of, wm: WhaleModel, ccds: Sequence[CCD], draws: Sequence, n: int, fun=None, seed: int = 0,
+                 summary: bool = True):
+    """``track`` with the DP tables from ``tables_of(model, f)`` (family f's
+    tables under ``model``, in the ``logpdf!`` layout), sampled on the host."""
+    import numpy as np
+
+    if len(draws) == 0:
+        raise ValueError("no posterior draws")
+    rng = np.random.default_rng(seed)
+    picks = rng.integers(len(draws), size=int(n))
+    trees = [[] for _ in ccds]
+    for j, i in enumerate(picks):
+        m = fun(wm, draws[i]) if fun is not None else wm(draws[i])
+        for f, c in enumerate(ccds):
+            trees[f] += backtrack_tables(m, c, tables_of(m, f), n=1, seed=_draw_seed(seed, j, f))
+    if not summary:
+        return trees
+    return [sumtrees(t, c, wm) for t, c in zip(trees, ccds)]
+
+
+def track(wm: WhaleModel, ccds: Sequence[CCD], draws: Sequence, n: int, fun=None, seed: int = 0,
+          summary: bool = True):
+    """``track(TreeTracker(wm, ccds, draws, fun), n)`` (src/track.jl:11-82):
+    ``n`` reconciled trees per family from the posterior predictive, each
+    under a draw picked uniformly from ``draws`` (``fun(wm, draw)`` gives the
+    model of a draw, by default ``wm(draw)``), summarised per family
+    (``sumtrees``) unless ``summary`` is false.
+
+    The loops run the other way round from the reference's, as its own
+    comment (src/track.jl:18-21) says would be faster: for each of the ``n``
+    picks, one batched ``logpdf!`` of every family on the device, then one
+    tree per family from its tables on the host.  All families of a pick share
+    its draw (the reference picks per family): each family's trees have the
+    same distribution.  The same seed gives the same trees."""
+    wm.load()
+    b = get_batch(wm, list(ccds), tables=True)
+    state = {"model": None}
+
+    def tables_of(m, f):
+        if state["model"] is not m:
+            b.logpdf(m)
+            state["model"] = m
+        return b.last_tables(f)[1]
+
+    return track_tables(tables_of, wm, ccds, draws, n, fun=fun, seed=seed, summary=summary)
