@@ -103,7 +103,7 @@ def test_track_from_oracle_tables(W, O):
         genes = _genes(wl.ale[f])
         for t in trees[f]:
             assert sorted(n.name for n in t.root.postwalk() if n.isleaf() and n.label != "loss") == genes
-    again = track_tables(tables_of, wm, ccds, [r], 6, seed=3, summary=False)
+    again = track_tables(tables_of, wm, ccds, [r], 6, seed=3, summary=False, threads=1)
     assert [[t.newick for t in x] for x in again] == [[t.newick for t in x] for x in trees]
     # two draws (the second with ten times the duplication rate): both are used
     hi = r(dict(λ=r.λ * 10))

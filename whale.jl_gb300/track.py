@@ -215,9 +215,15 @@ def _draw_seed(seed: int, j: int, f: int) -> int:
 
 
 def track_tables(tables_of, wm: WhaleModel, ccds: Sequence[CCD], draws: Sequence, n: int, fun=None, seed: int = 0,
-                 summary: bool = True):
+                 summary: bool = True, threads: int = 0):
     """``track`` with the DP tables from ``tables_of(model, f)`` (family f's
-    tables under ``model``, in the ``logpdf!`` layout), sampled on the host."""
+    tables under ``model``, in the ``logpdf!`` layout).  Per pick, the
+    families' tables are fetched in turn, then sampled on ``threads`` host
+    threads (0: every core); every tree has its own seed, so the trees do not
+    depend on the thread count."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+
     import numpy as np
 
     if len(draws) == 0:
@@ -225,17 +231,25 @@ def track_tables(tables_of, wm: WhaleModel, ccds: Sequence[CCD], draws: Sequence
     rng = np.random.default_rng(seed)
     picks = rng.integers(len(draws), size=int(n))
     trees = [[] for _ in ccds]
-    for j, i in enumerate(picks):
-        m = fun(wm, draws[i]) if fun is not None else wm(draws[i])
-        for f, c in enumerate(ccds):
-            trees[f] += backtrack_tables(m, c, tables_of(m, f), n=1, seed=_draw_seed(seed, j, f))
+    nt = max(1, min(threads or (os.cpu_count() or 1), len(ccds)))
+    with ThreadPoolExecutor(max_workers=nt) as pool:
+        for j, i in enumerate(picks):
+            m = fun(wm, draws[i]) if fun is not None else wm(draws[i])
+            tabs = [tables_of(m, f) for f in range(len(ccds))]
+            m.load()  # before the threads: they only read the model
+
+            def sample(f, m=m, tabs=tabs, j=j):
+                return backtrack_tables(m, ccds[f], tabs[f], n=1, seed=_draw_seed(seed, j, f))
+
+            for f, t in enumerate(pool.map(sample, range(len(ccds)))):
+                trees[f] += t
     if not summary:
         return trees
     return [sumtrees(t, c, wm) for t, c in zip(trees, ccds)]
 
 
 def track(wm: WhaleModel, ccds: Sequence[CCD], draws: Sequence, n: int, fun=None, seed: int = 0,
-          summary: bool = True):
+          summary: bool = True, threads: int = 0):
     """``track(TreeTracker(wm, ccds, draws, fun), n)`` (src/track.jl:11-82):
     ``n`` reconciled trees per family from the posterior predictive, each
     under a draw picked uniformly from ``draws`` (``fun(wm, draw)`` gives the
@@ -245,7 +259,8 @@ def track(wm: WhaleModel, ccds: Sequence[CCD], draws: Sequence, n: int, fun=None
     The loops run the other way round from the reference's, as its own
     comment (src/track.jl:18-21) says would be faster: for each of the ``n``
     picks, one batched ``logpdf!`` of every family on the device, then one
-    tree per family from its tables on the host.  All families of a pick share
+    tree per family from its tables on ``threads`` host threads (0: every
+    core).  All families of a pick share
     its draw (the reference picks per family): each family's trees have the
     same distribution.  The same seed gives the same trees."""
     wm.load()
@@ -258,4 +273,4 @@ def track(wm: WhaleModel, ccds: Sequence[CCD], draws: Sequence, n: int, fun=None
             state["model"] = m
         return b.last_tables(f)[1]
 
-    return track_tables(tables_of, wm, ccds, draws, n, fun=fun, seed=seed, summary=summary)
+    return track_tables(tables_of, wm, ccds, draws, n, fun=fun, seed=seed, summary=summary, threads=threads)
