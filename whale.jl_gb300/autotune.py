@@ -99,7 +99,8 @@ def tune(wm, ccds: Sequence, grad: bool = True, steps: int = 5, warmup: int = 2,
     ``grad``).  Returns ``(setting, batch, log)``: the knob values, the batch
     built with them (None when ``measure`` is given), and every
     (setting, ms per evaluation) tried.  ``measure`` replaces the device
-    timing (a function of the setting returning milliseconds)."""
+    timing (a function of the setting returning milliseconds).  Event timing
+    stays enabled on the context afterwards (``wg_ctx_set_timing``)."""
     from .core import Batch, default_context
 
     neighbours = dict(NEIGHBOURS if neighbours is None else neighbours)
