@@ -126,3 +126,22 @@ def test_track_from_oracle_tables(W, O):
     dup = sum(s.events["duplication"].sum() for s in sums)
     dup_lo = sum(s.events["duplication"].sum() for s in track_tables(tables_of, wm, ccds, [r], 40, seed=4))
     assert dup > dup_lo
+
+
+def test_pairwise_event_pps_sum_to_one(W, O, ex1_tree, ex1_files):
+    # test/runtests.jl:95-109 on the oracle's tables: 100 trees of the first
+    # example-1 family under DLWGD(λ = μ = ones, q = [0.2, 0.1], η = 0.9),
+    # Δt = 0.05; every gene pair's event probabilities sum to 1
+    from conftest import read
+    from whale_gb300.track import backtrack_tables, getpairs, sumtrees
+
+    t = W.readnw(ex1_tree)
+    wm = W.WhaleModel(W.DLWGD(λ=np.ones(17), μ=np.ones(17), q=[0.2, 0.1], η=0.9), t, 0.05)
+    ccd = W.read_ale(ex1_files[0], wm)[0]
+    om = O.OracleModel(ex1_tree, 0.05)
+    tab = om.family_tables(O.OracleCCD(om, read(ex1_files[0])), np.ones(17), np.ones(17), q=[0.2, 0.1], eta=0.9)
+    trees = backtrack_tables(wm, ccd, tab, n=100, seed=1)
+    fam, pairs, labels, pp = getpairs([sumtrees(trees, ccd, wm)], wm)[0]
+    assert len(pairs) == 13 * 12 // 2  # 13 genes
+    assert len(labels) == 2 * 17 + 3 * 2  # two labels per node, three per WGD node (19 nodes)
+    assert np.allclose(pp.sum(axis=1), 1.0)

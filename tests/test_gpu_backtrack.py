@@ -151,3 +151,15 @@ def test_track_matches_per_family_backtracking(W, fam):
     assert ll2 == ll and np.array_equal(tab2, tab)
     s = W.track(wm, ccds[:2], draws, 30, seed=2)
     assert all(abs(sum(fr for fr, _ in x.trees) - 1) < 1e-12 for x in s)
+
+
+def test_pairwise_event_pps_sum_to_one(W, ex1_tree, ex1_files):
+    # test/runtests.jl:95-109: 100 trees of the first example-1 family,
+    # summarised, and every gene pair's event probabilities sum to 1
+    t = W.readnw(ex1_tree)
+    wm = W.WhaleModel(W.DLWGD(λ=np.ones(17), μ=np.ones(17), q=[0.2, 0.1], η=0.9), t, 0.05)
+    ccd = W.read_ale(ex1_files[0], wm)[0]
+    trees = W.backtrack(wm, ccd, n=100, seed=1)
+    fam, pairs, labels, pp = W.getpairs([W.sumtrees(trees, ccd, wm)], wm)[0]
+    assert len(pairs) == 78 and len(labels) == 40
+    assert np.allclose(pp.sum(axis=1), 1.0)

@@ -17,7 +17,7 @@ from .core import (Batch, Context, default_context, get_batch, gradient, logpdf,
                    logpdf_plain, loglikelihood, map_gradient, nowhere_condition)
 from .mixture import MixtureModel, ModelArray
 from .autotune import tune
-from .track import RecNode, RecTree, TrackSummary, backtrack, sumtrees, track
+from .track import RecNode, RecTree, TrackSummary, backtrack, getpairs, sumtrees, track
 from .model import (ConstantDLWGD, DLWGD, NoCondition, NonExtinctCondition, NowhereExtinctCondition, RootCondition,
                     WhaleModel, condition)
 from .newick import (EXTREE, Node, addbranchwgds, copytree, extree, getlca, getleaves, getroot, insertnode, nwstr,
@@ -31,6 +31,6 @@ __all__ = [
     "CCD", "read_ale", "parse_ale_text", "logpdf", "logpdf_inplace", "logpdf_", "loglikelihood", "gradient",
     "logpdf_gradient", "logpdf_plain", "map_gradient", "Batch", "Context", "default_context", "get_batch",
     "readnw", "nwstr", "insertnode", "getlca", "getleaves", "getroot", "postwalk", "prewalk", "extree", "EXTREE",
-    "addbranchwgds", "copytree", "Node", "WhaleError", "MixtureModel", "ModelArray", "backtrack", "track", "sumtrees", "TrackSummary", "RecNode",
+    "addbranchwgds", "copytree", "Node", "WhaleError", "MixtureModel", "ModelArray", "backtrack", "track", "sumtrees", "getpairs", "TrackSummary", "RecNode",
     "RecTree", "tune",
 ]

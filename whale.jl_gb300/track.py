@@ -274,3 +274,53 @@ def track(wm: WhaleModel, ccds: Sequence[CCD], draws: Sequence, n: int, fun=None
         return b.last_tables(f)[1]
 
     return track_tables(tables_of, wm, ccds, draws, n, fun=fun, seed=seed, summary=summary, threads=threads)
+
+
+def pair_labels(wm: WhaleModel) -> List[str]:
+    """Event labels of ``getpairs`` (src/rectree.jl:52-62): per species node
+    (its id), ``<id>_duplication`` and ``<id>_wgd``, ``<id>_wgdloss`` for a WGD
+    node or ``<id>_speciation`` otherwise."""
+    out = []
+    for m in wm.order:
+        out.append(f"{m.id}_duplication")
+        out += [f"{m.id}_wgd", f"{m.id}_wgdloss"] if m.kind == N.NODE_WGD else [f"{m.id}_speciation"]
+    return out
+
+
+def _leaves(n: RecNode):
+    return [x for x in n.postwalk() if x.isleaf()]
+
+
+def getpairs(summaries: Sequence[TrackSummary], wm: WhaleModel, digits: int = 3):
+    """``getpairs`` (src/rectree.jl:52-97): for every pair of surviving genes
+    of a family, the posterior probability that the pair's split node in the
+    reconciled tree is each event on each species node (``pair_labels``),
+    rounded to ``digits`` as the reference does.  One (family, pairs, labels,
+    pp) tuple per summary: pp[p, l] for pair p (``"a__b"``, names sorted) and
+    label l; each row sums to 1 up to the rounding."""
+    import numpy as np
+
+    labels = pair_labels(wm)
+    lab_ix = {l: i for i, l in enumerate(labels)}
+    out = []
+    for s in summaries:
+        first = [x for x in _leaves(s.trees[0][1].root) if x.label != "loss"]
+        pairs = ["__".join(sorted([first[i].name, first[j].name])) for i in range(len(first)) for j in range(i)]
+        pix = {p: i for i, p in enumerate(pairs)}
+        pp = np.zeros((len(pairs), len(labels)))
+        for f, t in s.trees:
+            for n in t.root.postwalk():
+                if len(n.children) != 2:
+                    continue
+                a = [x for x in _leaves(n.children[0]) if x.label != "loss"]
+                b = [x for x in _leaves(n.children[1]) if x.label != "loss"]
+                if not a or not b:
+                    continue
+                col = lab_ix.get(f"{wm.order[n.node].id}_{n.label}")
+                if col is None:
+                    raise ValueError(f"pair split at a {n.label!r} node")
+                for x in a:
+                    for y in b:
+                        pp[pix["__".join(sorted([x.name, y.name]))], col] += f
+        out.append((s.fname, pairs, labels, np.round(pp, digits)))
+    return out
