@@ -13,6 +13,10 @@ Writes, next to this script:
                       above ATHA and above LCA(ATHA, ATRI), each new node
                       appended to its parent's children (insertnode!)
   example5/*.ale      example/example-5 CCDs, same treatment; example5_tree.nw
+  example4/*.ale      example/example-4/cytp450.ale (one family of 95 genes,
+                      4,916 clades), same treatment; example4_tree.nw
+  landplant/*.ale     docs/data/landplant/100fams (100 families), same
+                      treatment; landplant_tree.nw (its speciestree.nw)
   golden.json         the reference's own pinned values (test/runtests.jl:19,
                       :32) and the settings they were computed with
 """
@@ -40,7 +44,8 @@ def normalise(text: str) -> str:
 
 
 def main(ref: str) -> None:
-    for sub, dst in (("example/example-1/ale", "example1"), ("example/example-5", "example5")):
+    for sub, dst in (("example/example-1/ale", "example1"), ("example/example-5", "example5"),
+                     ("example/example-4", "example4"), ("docs/data/landplant/100fams", "landplant")):
         src = os.path.join(ref, sub)
         os.makedirs(os.path.join(HERE, dst), exist_ok=True)
         for f in sorted(os.listdir(src)):
@@ -60,6 +65,12 @@ def main(ref: str) -> None:
         t5 = fh.readline().strip()
     with open(os.path.join(HERE, "example5_tree.nw"), "w") as fh:
         fh.write(t5 + "\n")
+    for src, dst in (("example/example-4/tree.nw", "example4_tree.nw"),
+                     ("docs/data/landplant/speciestree.nw", "landplant_tree.nw")):
+        with open(os.path.join(ref, src)) as fh:
+            t = fh.readline().strip()
+        with open(os.path.join(HERE, dst), "w") as fh:
+            fh.write(t + "\n")
     golden = {
         "source": "test/runtests.jl of Whale.jl v2.1.0",
         "single_family": {"file": "OG0004512.fasta.nex.treesample.ale", "dt": 0.05, "maxn": 5,

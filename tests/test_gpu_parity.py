@@ -161,3 +161,33 @@ def test_results_do_not_depend_on_pack_threads(W, monkeypatch):
         del b
     for x, y in zip(*out):
         assert np.array_equal(np.asarray(x), np.asarray(y))
+
+
+@pytest.mark.parametrize("sub,tree", [("example4", "example4_tree.nw"), ("landplant", "landplant_tree.nw")])
+def test_real_data_against_oracle(W, O, sub, tree):
+    # the reference's own data (example/example-4: one family of 4,917 clades
+    # on a 44-taxon tree; docs/data/landplant/100fams: 100 families on 13
+    # taxa) under branch-wise rates: per-family log L within 1e-10 of the
+    # oracle and the gradient within 1e-8 of its duals
+    from conftest import GOLDEN, read
+
+    nw = read(os.path.join(GOLDEN, tree)).strip()
+    d = os.path.join(GOLDEN, sub)
+    files = [os.path.join(d, f) for f in sorted(os.listdir(d))]
+    t = W.readnw(nw)
+    n = len(W.postwalk(t))
+    rng = np.random.default_rng(11)
+    lam, mu = rng.normal(np.log(0.2), 0.3, n), rng.normal(np.log(0.25), 0.3, n)
+    wm = W.WhaleModel(W.DLWGD(λ=lam, μ=mu, η=0.7), t, 0.1)
+    ccds = W.read_ale(d, wm)
+    om = O.OracleModel(nw, 0.1)
+    occ = O.read_ale_files(om, files)
+    tot, per = W.Batch(wm, ccds).logpdf(wm, per_family=True)
+    otot, oper = om.logpdf(occ, lam, mu, q=[], eta=0.7)
+    assert np.all(np.isfinite(oper))
+    for a, b in zip(per, oper):
+        assert a == pytest.approx(b, rel=1e-10)
+    assert tot == pytest.approx(otot, rel=1e-10)
+    g = W.gradient(wm, ccds)
+    _, og = om.gradient(occ, lam, mu, q=[], eta=0.7)
+    assert np.max(np.abs(g - og) / np.maximum(np.abs(og), 1.0)) <= 1e-8

@@ -73,6 +73,34 @@ def test_ale_reader_matches_oracle(W, O, ex1_tree, ex1_files):
             assert a["nleaves"][i] == d["nleaves"] and a["counts"][i] == d["count"]
 
 
+@pytest.mark.parametrize("sub,tree", [("example4", "example4_tree.nw"), ("landplant", "landplant_tree.nw")])
+def test_real_data_parses_like_oracle(W, O, sub, tree):
+    # the reference's own data: example/example-4 (one family of 95 genes and
+    # 4,916 clades, 44-taxon tree) and docs/data/landplant/100fams (100
+    # families, 13 taxa): clades, splits and species equal the oracle's
+    nw = read(os.path.join(GOLDEN, tree)).strip()
+    d = os.path.join(GOLDEN, sub)
+    files = [os.path.join(d, f) for f in sorted(os.listdir(d))]
+    t = W.readnw(nw)
+    n = len(W.postwalk(t))
+    wm = W.WhaleModel(W.DLWGD(λ=np.zeros(n), μ=np.zeros(n), η=0.7), t, 0.1)
+    om = O.OracleModel(nw, 0.1)
+    ccds = W.read_ale(d, wm)
+    occ = O.read_ale_files(om, files)
+    assert len(ccds) == len(files) == (1 if sub == "example4" else 100)
+    for c, oc in zip(ccds, occ):
+        a = c.arrays()
+        assert (c.n_clades, c.n_triples) == (oc.n_clades, oc.n_triples)
+        so, spo = a["split_offsets"], a["species_offsets"]
+        for i in range(c.n_clades):
+            dd = oc.clade(i)
+            assert list(zip(a["g1"][so[i]:so[i + 1]].tolist(), a["g2"][so[i]:so[i + 1]].tolist(),
+                            a["p"][so[i]:so[i + 1]].tolist())) == dd["splits"]
+            assert a["species"][spo[i]:spo[i + 1]].tolist() == dd["species"]
+    if sub == "example4":
+        assert ccds[0].n_clades == 4917  # 4,916 clades and the ubiquitous one
+
+
 def test_set_sampling_probabilities(W, O):
     # test/runtests.jl:80-93: setsamplingp! gives every leaf its probability in
     # getθ; beyond that, a leaf's first ε is its p (src/model.jl:170), so the

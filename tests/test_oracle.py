@@ -105,3 +105,21 @@ def test_fixtures_equal_reference_files(O, ex1_tree, golden):
     m = O.OracleModel(ex1_tree, 0.05, condition="root")
     tot, per = m.logpdf(O.read_ale_files(m, files), np.ones(17), np.ones(17), q=[0.2, 0.1], eta=0.9)
     assert tot == pytest.approx(golden["twelve_families"]["logpdf"], rel=1e-12)
+
+
+@pytest.mark.skipif(not os.path.isdir(REFERENCE), reason="reference checkout not present")
+@pytest.mark.parametrize("sub,src,tree", [("example4", "example/example-4", "example4_tree.nw"),
+                                          ("landplant", "docs/data/landplant/100fams", "landplant_tree.nw")])
+def test_real_data_fixtures_equal_reference_files(O, sub, src, tree):
+    # the normalised fixtures give the same per-family likelihood as the files
+    nw = read(os.path.join(GOLDEN, tree)).strip()
+    m = O.OracleModel(nw, 0.1, condition="root")
+    n = int(m.nonwgd)
+    d = os.path.join(REFERENCE, src)
+    orig = [os.path.join(d, f) for f in sorted(os.listdir(d)) if f.endswith(".ale")]
+    mine = [os.path.join(GOLDEN, sub, os.path.basename(f)) for f in orig]
+    rates = (np.full(n, np.log(0.2)), np.full(n, np.log(0.25)))
+    _, a = m.logpdf(O.read_ale_files(m, orig), *rates, q=[], eta=0.7)
+    _, b = m.logpdf(O.read_ale_files(m, mine), *rates, q=[], eta=0.7)
+    assert np.array_equal(a, b) and np.all(np.isfinite(a))
+
