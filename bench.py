@@ -101,10 +101,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# DRAM bytes per evaluation of the 5,000-family workload, summed over the
-# launches of each kernel family, from the ncu launch list kept in
-# profiles/launches_cfg1_5000fam.txt (not measurable inside the timed run).
-NCU_DRAM_BYTES = {"adjoint": 758_141_440, "forward": 349_668_352}
+LAUNCH_PROFILE = os.path.join(ROOT, "profiles", "launches_cfg1_5000fam.txt")
+
+
+def ncu_traffic():
+    """DRAM bytes per evaluation of the 5,000-family workload by kernel
+    family, read from the committed ncu launch-list summary (its line
+    ``dram_bytes_per_evaluation: adjoint=<bytes> forward=<bytes>
+    commit=<sha>``); DRAM traffic cannot be measured inside the timed run."""
+    try:
+        with open(LAUNCH_PROFILE) as fh:
+            for line in fh:
+                if line.startswith("dram_bytes_per_evaluation:"):
+                    kv = dict(x.split("=", 1) for x in line.split(":", 1)[1].split())
+                    return {"adjoint": int(kv["adjoint"]), "forward": int(kv["forward"]),
+                            "commit": kv.get("commit")}
+    except (OSError, ValueError, KeyError):
+        pass
+    return None
 
 
 def workload(nf):
@@ -126,7 +140,7 @@ def cpu_reference(W, wl, ccds_idx, steps, warmup, threads):
     O.build()
     wm = wl.model
     om = O.OracleModel(W.nwstr(wm.tree), wm.Δt, minn=wm.minn, maxn=wm.maxn)
-    occ = [O.OracleCCD(om, wl.ale[i]) for i in ccds_idx]
+    occ = O.parse_texts(om, [wl.ale[i] for i in ccds_idx], threads)
     r = wm.rates
     rng = np.random.default_rng(123)
     times = []
@@ -139,6 +153,47 @@ def cpu_reference(W, wl, ccds_idx, steps, warmup, threads):
         if s >= warmup:
             times.append(dt)
     return len(occ) / float(np.mean(times)), times
+
+
+PARITY_LOGL = 1e-10  # per-family relative, as the benchmark spec states
+PARITY_GRAD = 1e-8   # relative to max(|g|, 1), against forward-mode duals
+
+
+def parity_check(W, wl, wm, batch, per_family, threads, n_grad=200):
+    """The timed workload checked against the oracle after the timed region:
+    every family's log L from the last timed step against the oracle's
+    value-only logpdf at the same rates, and the gradient of a seeded
+    n_grad-family sample (the same batch, weights 1 on the sample and 0
+    elsewhere, the condition scaled by the sample size) against the oracle's
+    forward-mode duals.  Returns the parity object of the bench line."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from whale_gb300.core import map_gradient
+
+    O.build()
+    om = O.OracleModel(W.nwstr(wm.tree), wm.Δt, minn=wm.minn, maxn=wm.maxn)
+    occ = O.parse_texts(om, wl.ale, threads)
+    r = wm.rates
+    _, oper = om.logpdf(occ, r.λ, r.μ, q=r.q, eta=r.η, nthreads=threads)
+    a, b = np.asarray(per_family, float), np.asarray(oper, float)
+    both_inf = np.isneginf(a) & np.isneginf(b)
+    rel = np.where(both_inf, 0.0, np.abs(a - b) / np.maximum(np.abs(b), 1e-300))
+    sample = np.sort(np.random.default_rng(11).choice(len(occ), size=min(n_grad, len(occ)), replace=False))
+    w = np.zeros(len(occ))
+    w[sample] = 1.0
+    _, _, dl, dm, dq, de = batch.grad_nodes_weighted(wm, w, float(len(sample)))
+    g = map_gradient(wm, dl, dm, dq, de)
+    flat = np.concatenate([g["λ"], g["μ"], g["q"], [g["η"]]])
+    _, og = om.gradient([occ[i] for i in sample], r.λ, r.μ, q=r.q, eta=r.η, nthreads=threads)
+    grel = np.abs(flat - og) / np.maximum(np.abs(og), 1.0)
+    out = {"max_rel_logl": float(np.max(rel)), "max_rel_grad": float(np.max(grel)),
+           "families_checked": int(len(occ)), "families_grad_checked": int(len(sample)),
+           "minus_inf_families": int(np.sum(both_inf)),
+           "bars": {"logl": PARITY_LOGL, "grad": PARITY_GRAD},
+           "against": "oracle/whale_oracle.cpp (value-only logpdf on all families; duals of chunk 12 on the "
+                      "sample) at the rates of the last timed step"}
+    out["ok"] = bool(out["max_rel_logl"] <= PARITY_LOGL and out["max_rel_grad"] <= PARITY_GRAD)
+    return out
 
 
 def pick_cpu_sample(W, wl, budget_s, threads):
@@ -154,7 +209,7 @@ def pick_cpu_sample(W, wl, budget_s, threads):
     r = wm.rates
     # time a probe of 32 families, then scale the sample to the budget
     probe = list(order[:32])
-    occ = [O.OracleCCD(om, wl.ale[i]) for i in probe]
+    occ = O.parse_texts(om, [wl.ale[i] for i in probe], threads)
     t0 = time.perf_counter()
     om.gradient(occ, r.λ, r.μ, q=r.q, eta=r.η, nthreads=threads)
     per = (time.perf_counter() - t0) / len(probe)
@@ -169,10 +224,11 @@ def run_reference(args, W, rank):
 
     wl = synth.config1(n_families=args.families)
     threads = os.cpu_count() or 1
-    # each step a bounded sample: the whole run about two minutes of CPU work
-    # (at most 0.5 s per step; at 1,000 steps still ~800 families per step,
+    # each step the whole workload when the run fits in about two minutes of
+    # CPU work (a 20-step run on the 16-core host does), else a bounded
+    # random sample of it (at 1,000 steps still ~800 families per step,
     # enough to keep every host thread busy)
-    per_step = max(0.03, min(0.5, 120.0 / max(1, args.steps + args.warmup)))
+    per_step = max(0.03, 120.0 / max(1, args.steps + args.warmup))
     idx = pick_cpu_sample(W, wl, per_step, threads)
     v, times = cpu_reference(W, wl, idx, args.steps, args.warmup, threads)
     # the same on one core, for the single-thread figure (a smaller sample)
@@ -186,12 +242,15 @@ def run_reference(args, W, rank):
                    "families_in_sample": len(idx),
                    "method": "logL + gradient by forward-mode duals of chunk 12 on host cores"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{len(idx)} of {args.families} families (random, seed 7) per step"},
+                         "sample": (f"all {args.families} families per step" if len(idx) == args.families else
+                                    f"{len(idx)} of {args.families} families (random, seed 7) per step")},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "cpu_one_core": {"value": v1, "unit": UNIT, "cores": 1,
                          "sample": f"{len(idx1)} of {args.families} families (random, seed 7), one step"},
         "note": "Julia is not available, so the reference itself cannot run; this is the C++ restatement "
-                "of its logpdf + ForwardDiff gradient (oracle/whale_oracle.cpp), OpenMP over families",
+                "of its logpdf + ForwardDiff gradient (oracle/whale_oracle.cpp), OpenMP over families; the "
+                "workload is generated by the library's host parts (libwhalehost.so), the GPU library is "
+                "not loaded",
     }
     print(json.dumps(line), flush=True)
 
@@ -210,6 +269,10 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = dist_env()
+    if args.impl == "reference":
+        # the workload is generated by the library's host parts alone: this
+        # arm never loads the GPU library
+        os.environ["WG_HOST_LIBRARY"] = "1"
     import __graft_entry__
 
     W = __graft_entry__.load_package()
@@ -273,7 +336,8 @@ def main():
 
     for _ in range(args.warmup):
         step(inputs(perturbed(W, wm, rng)))
-    models = [inputs(perturbed(W, wm, rng)) for _ in range(args.steps)]
+    step_models = [perturbed(W, wm, rng) for _ in range(args.steps)]
+    models = [inputs(m) for m in step_models]
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
@@ -294,6 +358,10 @@ def main():
     if pg:
         pg.barrier()
     clk = clocks.stop()
+    # parity of the timed workload: the last step's per-family log L (still in
+    # the caller's buffer) against the oracle at that step's rates
+    threads = os.cpu_count() or 1
+    parity = parity_check(W, wl, step_models[-1], batch, per_b.copy(), threads)
     dev_step = float(np.mean(dev_ms))
     wall_step = wall / args.steps
     nfw, ngr = W._native.C.c_int32(), W._native.C.c_int32()
@@ -337,21 +405,26 @@ def main():
                  "what": "plain path (one family per launch) differentiated by central differences"}
     # roofline of the dominant kernel (the adjoint or the forward)
     fa = float(np.mean(a_ms)), float(np.mean(f_ms))
+    prof = ncu_traffic() if NF == 5000 else None
     if fa[0] >= fa[1]:
         kname, kms, kflops = "k_adj2 (all levels and size classes)", fa[0], batch.flops_adj
-        traffic = NCU_DRAM_BYTES["adjoint"] if NF == 5000 else None
+        traffic = prof["adjoint"] if prof else None
     else:
         kname, kms, kflops = "k_fwd2<true> (all levels and size classes)", fa[1], batch.flops_fwd
-        traffic = NCU_DRAM_BYTES["forward"] if NF == 5000 else None
+        traffic = prof["forward"] if prof else None
     achieved = kflops / (kms * 1e-3) / 1e12
     roof = {"bound": "fp64", "kernel": kname, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
             "frac": achieved / fp64_peak if fp64_peak else None, "traffic": traffic,
             "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum over the kernel's launches of one "
-                              "evaluation, one ncu capture of this workload (profiles/launches_cfg1_5000fam.txt)",
+                              "evaluation, one ncu capture of this workload (profiles/launches_cfg1_5000fam.txt"
+                              + (f", commit {prof['commit']}" if prof and prof.get("commit") else "") + ")",
             "peak_source": "measured in this run: register-resident DFMA loop (wg_probe_fp64); "
                            "MEASURED_PEAKS.json has no FP64 figure",
-            "algorithmic_flops_per_launch": kflops, "launch_ms": kms,
-            "hbm_gbs_algorithmic": batch.bytes_fwd / (fa[1] * 1e-3) / 1e9}
+            "algorithmic_flops_per_launch": kflops, "launch_ms": kms}
+    # the forward's own HBM figure: its algorithmic bytes over its own time
+    fwd_hbm = {"kernel": "k_fwd2<true> (all levels and size classes)", "algorithmic_bytes": batch.bytes_fwd,
+               "ms": fa[1], "gbs": batch.bytes_fwd / (fa[1] * 1e-3) / 1e9,
+               "traffic": prof["forward"] if prof else None}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_step, "higher_is_better": True, "scaling": "weak",
@@ -372,9 +445,11 @@ def main():
                       "reduce": float(np.mean(r_ms)), "forward_only": fwd_only_ms},
         "grad_cost_vs_forward": dev_step / fwd_only_ms,
         "roofline": roof,
+        "forward_hbm": fwd_hbm,
         "plain_fd": plain,
         "speedup_vs_plain_fd": (value / plain["value"]) if plain else None,
         "clocks": clk,
+        "parity": parity,
     }
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -388,6 +463,10 @@ def main():
     if pg:
         pg.barrier()
         pg.destroy_process_group()
+    if not parity["ok"]:
+        print(f"parity broken: max_rel_logl {parity['max_rel_logl']:.3e} (bar {PARITY_LOGL:g}), "
+              f"max_rel_grad {parity['max_rel_grad']:.3e} (bar {PARITY_GRAD:g})", file=sys.stderr, flush=True)
+        sys.exit(3)
 
 
 if __name__ == "__main__":

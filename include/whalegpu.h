@@ -226,10 +226,12 @@ int wg_batch_tables(wg_ctx* ctx, wg_batch* b, int32_t family, double* out, int64
  * needs -- the top row of every (node, family group) task -- lives in one
  * fixed device array of 1 << 20 doubles (8 MiB) that every GPU loading the
  * library holds until exit; batches needing more are rejected with WG_ERANGE.
- * The first call on a device looks up that array's address (no allocation),
- * so make it before any stream capture.  All calls share the array and it
- * keeps the last call's contents: calls whose work overlaps on the GPU (two
- * host threads, two contexts on one device) race on it. */
+ * wg_ctx_create looks up that array's device address once (the library's
+ * kernels are loaded by then, so the lookup allocates nothing); this call
+ * only uses it.  An evaluation enqueued by wg_enqueue must be fetched first
+ * (WG_ESTATE otherwise).  All calls share the array and it keeps the last
+ * call's contents: calls whose work overlaps on the GPU (two host threads,
+ * two contexts on one device) race on it. */
 int wg_logpdf_noalloc(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, double* total);
 
 /* backtrack (src/track.jl:180-488): samples n_samples reconciled gene trees

@@ -172,3 +172,13 @@ def read_ale_files(model: OracleModel, paths):
         with open(pth) as fh:
             out.append(OracleCCD(model, fh.read(), os.path.basename(pth)))
     return out
+
+
+def parse_texts(model: OracleModel, texts, threads: int = 0):
+    """OracleCCDs of many ALE texts, parsed on host threads (ctypes releases
+    the GIL during each parse); results in input order."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    n = threads or os.cpu_count() or 1
+    with ThreadPoolExecutor(max_workers=n) as ex:
+        return list(ex.map(lambda s: OracleCCD(model, s), texts))

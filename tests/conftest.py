@@ -5,7 +5,9 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REFERENCE = "/root/reference"  # the reference checkout, present only where fixtures are regenerated
+# the reference checkout, named by WHALE_REFERENCE_DIR where the fixtures are
+# regenerated or re-checked against it (unset elsewhere: those tests skip)
+REFERENCE = os.environ.get("WHALE_REFERENCE_DIR", "")
 
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))

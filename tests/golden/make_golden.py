@@ -85,4 +85,7 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("WHALE_REFERENCE_DIR", "")
+    if not src:
+        sys.exit("usage: make_golden.py <reference checkout> (or set WHALE_REFERENCE_DIR)")
+    main(src)

@@ -191,3 +191,33 @@ def test_real_data_against_oracle(W, O, sub, tree):
     g = W.gradient(wm, ccds)
     _, og = om.gradient(occ, lam, mu, q=[], eta=0.7)
     assert np.max(np.abs(g - og) / np.maximum(np.abs(og), 1.0)) <= 1e-8
+
+
+def test_config1_full_batch(W, O):
+    # the bench's timed workload as the bench packs it (all 5,000 config-1
+    # families in one gradient batch): every family's log L from the
+    # gradient evaluation within 1e-10 of the oracle, and the gradient of a
+    # 200-family sample (weights 1 on the sample, 0 elsewhere, the condition
+    # scaled by the sample size) within 1e-8 of the oracle's duals
+    from whale_gb300 import synth
+    from whale_gb300.core import map_gradient
+
+    wl = synth.config1(seed=1, n_families=5000)
+    wm = wl.model
+    b = W.Batch(wm, wl.ccds(), grad=True)
+    tot, per, *_ = b.grad_nodes(wm)
+    om = O.OracleModel(W.nwstr(wm.tree), wm.Δt, minn=wm.minn, maxn=wm.maxn)
+    occ = O.parse_texts(om, wl.ale)
+    r = wm.rates
+    otot, oper = om.logpdf(occ, r.λ, r.μ, q=r.q, eta=r.η)
+    assert len(per) == 5000
+    assert np.max(_rel(per, oper)) <= REL
+    assert tot == pytest.approx(otot, rel=REL)
+    sample = np.sort(np.random.default_rng(11).choice(5000, size=200, replace=False))
+    w = np.zeros(5000)
+    w[sample] = 1.0
+    _, _, dl, dm, dq, de = b.grad_nodes_weighted(wm, w, 200.0)
+    g = map_gradient(wm, dl, dm, dq, de)
+    flat = np.concatenate([g["λ"], g["μ"], g["q"], [g["η"]]])
+    _, og = om.gradient([occ[i] for i in sample], r.λ, r.μ, q=r.q, eta=r.η)
+    assert np.max(np.abs(flat - og) / np.maximum(np.abs(og), 1.0)) <= 1e-8

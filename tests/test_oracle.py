@@ -97,7 +97,7 @@ def test_discretisation_stable(O):
         assert np.all(np.abs(np.array(vals) - vals[0]) < 0.1)
 
 
-@pytest.mark.skipif(not os.path.isdir(REFERENCE), reason="reference checkout not present")
+@pytest.mark.skipif(not REFERENCE or not os.path.isdir(REFERENCE), reason="WHALE_REFERENCE_DIR not set")
 def test_fixtures_equal_reference_files(O, ex1_tree, golden):
     # the normalised fixtures give the same likelihood as the reference's files
     src = os.path.join(REFERENCE, "example", "example-1", "ale")
@@ -107,7 +107,7 @@ def test_fixtures_equal_reference_files(O, ex1_tree, golden):
     assert tot == pytest.approx(golden["twelve_families"]["logpdf"], rel=1e-12)
 
 
-@pytest.mark.skipif(not os.path.isdir(REFERENCE), reason="reference checkout not present")
+@pytest.mark.skipif(not REFERENCE or not os.path.isdir(REFERENCE), reason="WHALE_REFERENCE_DIR not set")
 @pytest.mark.parametrize("sub,src,tree", [("example4", "example/example-4", "example4_tree.nw"),
                                           ("landplant", "docs/data/landplant/100fams", "landplant_tree.nw")])
 def test_real_data_fixtures_equal_reference_files(O, sub, src, tree):

@@ -57,3 +57,65 @@ def test_noalloc_rejects_batches_beyond_its_scratch(W):
     with pytest.raises(W.WhaleError) as ei:
         _noalloc(N, b, wm, b.n)
     assert ei.value.code == N.WG_ERANGE and "scratch" in str(ei.value)
+
+
+def test_noalloc_refuses_while_an_enqueued_evaluation_is_unfetched(W):
+    # an evaluation enqueued with wg_enqueue owns the batch's result buffers
+    # until wg_fetch: the allocation-free call is refused meanwhile, and the
+    # fetch then returns the enqueued evaluation's own results
+    from whale_gb300 import _native as N
+    from whale_gb300 import synth
+
+    wl = synth.config0(seed=5, n_families=40)
+    wm = wl.model
+    b = W.Batch(wm, wl.ccds())
+    ref_tot, ref_per = b.logpdf(wm, per_family=True)
+    L = N.lib()
+    wm.load()
+    N.check(L.wg_enqueue(b.ctx.h, wm._struct.h, b.h, 0))
+    with pytest.raises(W.WhaleError) as ei:
+        _noalloc(N, b, wm, b.n)
+    assert ei.value.code == N.WG_ESTATE
+    per = np.zeros(b.n)
+    tot = N.dbl()
+    N.check(L.wg_fetch(b.ctx.h, wm._struct.h, b.h, N.dptr(per), ctypes.byref(tot), None, None, None, None))
+    assert np.array_equal(per, ref_per)
+    assert tot.value == ref_tot
+    # and once fetched, the call goes through
+    tot2, per2 = _noalloc(N, b, wm, b.n)
+    assert np.max(np.abs(per2 - ref_per) / np.abs(ref_per)) <= REL
+
+
+def test_noalloc_nowhere_extinct_condition(W):
+    # the total under NowhereExtinctCondition (condition on the host here, on
+    # the device in wg_logpdf) agrees with the batched entry point
+    from whale_gb300 import _native as N
+    from whale_gb300 import synth
+
+    wl = synth.config0(seed=6, n_families=30)
+    base = wl.model
+    wm = W.WhaleModel(base.rates, base.tree, base.Δt, condition=W.NowhereExtinctCondition(base.tree))
+    ccds = [W.parse_ale_text(a, wm) for a in wl.ale]
+    b = W.Batch(wm, ccds)
+    ref_tot, ref_per = b.logpdf(wm, per_family=True)
+    for _ in range(2):
+        tot, per = _noalloc(N, b, wm, b.n)
+        assert np.max(np.abs(per - ref_per) / np.abs(ref_per)) <= REL
+        assert tot == pytest.approx(ref_tot, rel=REL)
+
+
+def test_noalloc_rows_in_device_memory(W):
+    # every task forced onto the device-memory rows path: the allocation-free
+    # call launches those kernel variants too
+    from whale_gb300 import _native as N
+    from whale_gb300 import synth
+
+    wl = synth.config1(seed=3, n_families=60)
+    wm = wl.model
+    ccds = [c for c in wl.ccds() if c.n_clades <= 600]
+    b = W.Batch(wm, ccds, scratch_rows=True)
+    ref_tot, ref_per = b.logpdf(wm, per_family=True)
+    for _ in range(2):
+        tot, per = _noalloc(N, b, wm, b.n)
+        assert np.max(np.abs(per - ref_per) / np.abs(ref_per)) <= REL
+        assert tot == pytest.approx(ref_tot, rel=REL)

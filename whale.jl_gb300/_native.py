@@ -2,6 +2,9 @@
 
 The library is built in-tree by ``build.py``.  There is no fallback: if the
 shared object is missing or fails to load, every call that needs it raises.
+With WG_HOST_LIBRARY=1 in the environment the host parts alone are loaded
+(libwhalehost.so: model, ALE reader, packer, workload generator, tracking);
+the device entry points are then absent and calling one raises.
 """
 from __future__ import annotations
 
@@ -89,7 +92,10 @@ def _declare(L):
         "wg_synth_family": (C.c_int, [vp, P_dbl, P_dbl, P_dbl, dbl, C.POINTER(C.c_char_p), u64, i32, i32, i32, i32,
                                       i32, C.c_char_p, i64, P_i64]),
     }
+    host_only = os.path.basename(getattr(L, "_name", "") or "") == os.path.basename(_build.HOST_LIB)
     for name, (res, args) in sigs.items():
+        if host_only and not hasattr(L, name):
+            continue  # a device entry point: absent from the host library
         f = getattr(L, name)
         f.restype = res
         f.argtypes = args
@@ -100,9 +106,10 @@ def lib():
     """Load (building first if needed) libwhalegpu.so; raises if it cannot."""
     global _lib
     if _lib is None:
-        path = _build.LIB
+        host_only = os.environ.get("WG_HOST_LIBRARY") == "1"
+        path = _build.HOST_LIB if host_only else _build.LIB
         if not os.path.exists(path):
-            path = _build.build()
+            _build.build()
         _lib = _declare(C.CDLL(path))
     return _lib
 

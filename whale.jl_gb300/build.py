@@ -16,6 +16,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libwhalegpu.so")
+# the host parts alone (model, ALE reader, packer, workload generator,
+# tracking; no CUDA): for processes that must not load the GPU library
+HOST_LIB = os.path.join(OUT, "libwhalehost.so")
 
 CXX_SRCS = ["wg_api.cpp", "wg_model.cpp", "wg_ccd.cpp", "wg_pack.cpp", "wg_synth.cpp", "wg_track.cpp"]
 CU_SRCS = ["wg_kernels.cu", "wg_nowhere.cu"]
@@ -81,6 +84,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         if r.returncode != 0:
             raise RuntimeError("libwhalegpu link failed:\n" + r.stdout)
+    host_objs = objs[: len(CXX_SRCS)]
+    if force or jobs or _stale(HOST_LIB, host_objs):
+        cmd = ["g++", "-shared", "-o", HOST_LIB, *host_objs, "-Wl,--no-undefined", "-lpthread"]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("libwhalehost link failed:\n" + r.stdout)
     return LIB
 
 

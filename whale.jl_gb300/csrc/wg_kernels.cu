@@ -19,7 +19,6 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
-#include <mutex>
 #include <string>
 
 #include "wg_internal.h"
@@ -1284,6 +1283,7 @@ struct wg_ctx {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   float last_ms[3] = {0, 0, 0};
   std::unique_ptr<NwPlan> nw;  // wg_nowhere_condition's plan
+  double* noalloc_tops = nullptr;  // device address of wg_logpdf_noalloc's fixed scratch on this device
 };
 
 namespace {
@@ -2043,6 +2043,22 @@ void fetch_plain(PlainBatch* b, const wg_model* m, double* per_family, double* t
          nullptr, nullptr);
 }
 
+// Fixed device scratch of wg_logpdf_noalloc (the top row of every task):
+// 1 << 20 doubles (8 MiB), held by every device that loads the library.
+constexpr int64_t kNoAllocMaxTops = (int64_t)1 << 20;
+__device__ __align__(256) double g_noalloc_tops[kNoAllocMaxTops];
+
+// In host code g_noalloc_tops names a host-side stand-in, not device memory:
+// its device address is looked up with the context's device current, when
+// the context is created (the module holding it is loaded by then, so the
+// lookup allocates nothing), and kept in the context.  A context created
+// after a device reset looks it up again.
+void noalloc_resolve(wg_ctx* c) {
+  void* p = nullptr;
+  ck(cudaGetSymbolAddress(&p, g_noalloc_tops), "cudaGetSymbolAddress(g_noalloc_tops)");
+  c->noalloc_tops = static_cast<double*>(p);
+}
+
 }  // namespace
 
 extern "C" {
@@ -2075,6 +2091,7 @@ int wg_ctx_create(int device, wg_ctx** out) {
     ck(cudaFuncSetAttribute(k_fwd2<true, kNT2L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
     ck(cudaFuncSetAttribute(k_adj2<kNT2L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
     ck(cudaFuncSetAttribute(k_adj2<kNT2H>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    noalloc_resolve(c.get());
     *out = c.release();
   });
 }
@@ -2362,31 +2379,10 @@ int wg_fetch(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, double* 
 // wg_logpdf allocates nothing per call either,
 // but its first call on a batch instantiates a CUDA graph, which does.  This
 // entry point runs the same forward task kernel with its scratch (the top
-// row of every task, read by the parent tasks) in the file-scope array below
+// row of every task, read by the parent tasks) in the file-scope array
+// g_noalloc_tops (its device address looked up when the context was created)
 // instead of the batch's own buffer, and launches the levels directly.
 // ===========================================================================
-namespace {
-
-constexpr int64_t kNoAllocMaxTops = (int64_t)1 << 20;  // doubles (8 MiB), held by every device that loads the library
-__device__ __align__(256) double g_noalloc_tops[kNoAllocMaxTops];
-
-// Device address of g_noalloc_tops, looked up once per device (with that
-// device current) on the first call there.
-double* noalloc_scratch(int device) {
-  static std::mutex mu;
-  static double* addr[64] = {};
-  if (device < 0 || device >= 64) throw Error(WG_EINVAL, "device index out of range");
-  std::lock_guard<std::mutex> lock(mu);
-  if (!addr[device]) {
-    void* p = nullptr;
-    ck(cudaGetSymbolAddress(&p, g_noalloc_tops), "cudaGetSymbolAddress(g_noalloc_tops)");
-    addr[device] = static_cast<double*>(p);
-  }
-  return addr[device];
-}
-
-}  // namespace
-
 extern "C" int wg_logpdf_noalloc(wg_ctx* ctx, wg_model* m, wg_batch* b, double* per_family, double* total) {
   WG_GUARD({
     if (!ctx || !m || !b || b->ctx != ctx) throw Error(WG_EINVAL, "wg_logpdf_noalloc: bad arguments");
@@ -2397,10 +2393,12 @@ extern "C" int wg_logpdf_noalloc(wg_ctx* ctx, wg_model* m, wg_batch* b, double* 
       throw Error(WG_ERANGE, "wg_logpdf_noalloc: the batch needs " + std::to_string(need) +
                                  " doubles of scratch, more than the fixed " + std::to_string(kNoAllocMaxTops) +
                                  " (split the families over smaller batches)");
+    // an enqueued evaluation owns the batch's result buffers until wg_fetch
+    if (b->pending) throw Error(WG_ESTATE, "wg_logpdf_noalloc: an enqueued evaluation of this batch is not fetched yet");
     ck(cudaSetDevice(ctx->device), "cudaSetDevice");
-    double* scratch = noalloc_scratch(ctx->device);
+    double* scratch = ctx->noalloc_tops;
+    if (!scratch) throw Error(WG_ESTATE, "wg_logpdf_noalloc: context has no scratch address");
     cudaStream_t s = ctx->stream;
-    if (b->pending) ck(cudaStreamSynchronize(s), "pending evaluation");
     b->tables_fresh = false;  // writes no tables; h_logl becomes this call's
     stage_params(b, m);
     ck(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(double) * (b->P + 2), cudaMemcpyHostToDevice, s),
