@@ -38,6 +38,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "families·(logL+grad)/s FP64 @17 taxa: batched adjoint vs plain GPU, rel err ≤1e-10"
+METRIC4 = "families·(logL+grad)/s FP64 @40 taxa (50,000 families, 10 WGDs, Δt=0.01), rel err ≤1e-10"
 UNIT = "families/s"
 
 
@@ -121,9 +122,19 @@ def ncu_traffic():
     return None
 
 
-def workload(nf):
+def workload(nf, config=1):
+    if config == 4:
+        return (f"cfg4: {nf:,} families, 40-taxon Yule tree + 10 WGDs, Δt=0.01, DLWGD log-normal rates, CCDs from "
+                "500 NNI-perturbed trees (heavy-tailed clade counts, widest rows in device memory); "
+                "log-likelihood + gradient (169 parameters) per step")
     return (f"cfg1: {nf:,} families, 17-taxon Yule tree + 3 WGDs, Δt=0.02, DLWGD log-normal rates; "
             "log-likelihood + gradient (70 parameters) per step")
+
+
+def make_workload(synth, config, families, rank):
+    if config == 4:
+        return synth.config4(n_families=families)
+    return synth.config1(seed=1 + rank, n_families=families)
 
 
 def perturbed(W, wm, rng, scale=0.01):
@@ -178,7 +189,10 @@ def parity_check(W, wl, wm, batch, per_family, threads, n_grad=200):
     a, b = np.asarray(per_family, float), np.asarray(oper, float)
     both_inf = np.isneginf(a) & np.isneginf(b)
     rel = np.where(both_inf, 0.0, np.abs(a - b) / np.maximum(np.abs(b), 1e-300))
-    sample = np.sort(np.random.default_rng(11).choice(len(occ), size=min(n_grad, len(occ)), replace=False))
+    # the gradient sample among families whose likelihood is representable
+    # (an underflowing family contributes nothing to the gradient)
+    fin = np.where(np.isfinite(b))[0]
+    sample = np.sort(np.random.default_rng(11).choice(fin, size=min(n_grad, len(fin)), replace=False))
     w = np.zeros(len(occ))
     w[sample] = 1.0
     _, _, dl, dm, dq, de = batch.grad_nodes_weighted(wm, w, float(len(sample)))
@@ -222,7 +236,7 @@ def run_reference(args, W, rank):
         return
     from whale_gb300 import synth
 
-    wl = synth.config1(n_families=args.families)
+    wl = make_workload(synth, args.config, args.families, 0)
     threads = os.cpu_count() or 1
     # each step the whole workload when the run fits in about two minutes of
     # CPU work (a 20-step run on the 16-core host does), else a bounded
@@ -235,10 +249,10 @@ def run_reference(args, W, rank):
     idx1 = pick_cpu_sample(W, wl, 2.0, 1)
     v1, _ = cpu_reference(W, wl, idx1, 1, 0, 1)
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "impl": "reference", "metric": METRIC4 if args.config == 4 else METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload(args.families), "families": args.families,
+        "config": {"workload": workload(args.families, args.config), "families": args.families,
                    "families_in_sample": len(idx),
                    "method": "logL + gradient by forward-mode duals of chunk 12 on host cores"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
@@ -261,11 +275,19 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)  # config 3: 1,000 successive evaluations
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--families", type=int, default=5000)
+    ap.add_argument("--config", type=int, default=1, choices=[1, 4],
+                    help="1: 5,000 families on 17 taxa (default); 4: 50,000 families on 40 taxa")
+    ap.add_argument("--families", type=int, default=None, help="default: 5,000 (config 1), 50,000 (config 4)")
+    ap.add_argument("--checkpoint", action="store_true",
+                    help="force per-level recomputation of the adjoint's tables (otherwise only past the budget)")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for the CPU leg")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     args = ap.parse_args()
+    if args.families is None:
+        args.families = 50000 if args.config == 4 else 5000
+    if args.config == 4:
+        args.no_plain = True  # one launch per family for 50,000 families; its widest families exceed shared memory
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = dist_env()
@@ -290,12 +312,14 @@ def main():
         pg = dist
     from whale_gb300 import synth
 
-    wl = synth.config1(seed=1 + rank, n_families=args.families)
+    t0 = time.perf_counter()
+    wl = make_workload(synth, args.config, args.families, rank)
     wm = wl.model
     ccds = wl.ccds()
+    gen_s = time.perf_counter() - t0
     ctx = W.Context(local)
     t0 = time.perf_counter()
-    batch = W.Batch(wm, ccds, grad=True, ctx=ctx)
+    batch = W.Batch(wm, ccds, grad=True, ctx=ctx, checkpoint=args.checkpoint)
     pack_s = time.perf_counter() - t0
     L = W._native.lib()
     W._native.check(L.wg_ctx_set_timing(ctx.h, 1))
@@ -322,10 +346,10 @@ def main():
                 N_.C.byref(de_b), None, None, None)
     t_ptrs = (N_.C.byref(fms), N_.C.byref(ams), N_.C.byref(rms))
 
-    def step(rates):
+    def step(rates, bh=None):
         _, lam, mu, q, eta, pp = rates
         N_.check(L.wg_model_set_rates(hm, lam, mu, q, eta, pp))
-        N_.check(L.wg_logpdf_grad(ctx.h, hm, batch.h, *out_ptrs))
+        N_.check(L.wg_logpdf_grad(ctx.h, hm, bh or batch.h, *out_ptrs))
         N_.check(L.wg_ctx_timings(ctx.h, *t_ptrs))
         return tot_b.value, fms.value, ams.value, rms.value
 
@@ -361,7 +385,8 @@ def main():
     # parity of the timed workload: the last step's per-family log L (still in
     # the caller's buffer) against the oracle at that step's rates
     threads = os.cpu_count() or 1
-    parity = parity_check(W, wl, step_models[-1], batch, per_b.copy(), threads)
+    parity_per = per_b.copy()
+    parity = parity_check(W, wl, step_models[-1], batch, parity_per, threads)
     dev_step = float(np.mean(dev_ms))
     wall_step = wall / args.steps
     nfw, ngr = W._native.C.c_int32(), W._native.C.c_int32()
@@ -426,10 +451,10 @@ def main():
                "ms": fa[1], "gbs": batch.bytes_fwd / (fa[1] * 1e-3) / 1e9,
                "traffic": prof["forward"] if prof else None}
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": METRIC4 if args.config == 4 else METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload(NF),
+        "config": {"workload": workload(NF, args.config),
                    "families": NF, "clades_mean": float(np.mean([c.n_clades for c in ccds])),
                    "clades_max": int(max(c.n_clades for c in ccds)),
                    "triples_mean": float(np.mean([c.n_triples for c in ccds])), "slices": NR,
@@ -437,7 +462,9 @@ def main():
                    "l2": "inputs exceed L2: sum programs + DP tables resident in HBM "
                          f"({batch.device_bytes / 1e9:.2f} GB > 129 MB)",
                    "parallelism": f"replicas x{world} (weak scaling)" if world > 1 else "single GPU",
-                   "pack_seconds": pack_s},
+                   "pack_seconds": pack_s, "generate_seconds": gen_s,
+                   "tables": dict(zip(("size_classes", "classes_recomputing_tables", "full_bytes", "held_bytes"),
+                                      (lambda t: (t[0], t[1], 8 * t[2], 8 * t[3]))(batch.tables_layout())))},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": wall_step_ms},
         "gpu_launches": n_launch * args.steps,
@@ -451,6 +478,29 @@ def main():
         "clocks": clk,
         "parity": parity,
     }
+    if args.config == 4 and not args.checkpoint:
+        # the same steps on the per-level recomputation layout (what a batch
+        # uses by itself once its tables exceed the device-memory budget)
+        del batch
+        ckb = W.Batch(wm, ccds, grad=True, ctx=ctx, checkpoint=True)
+        for m in models[: args.warmup]:
+            step(m, ckb.h)
+        ck_ms = []
+        for m in models:
+            _, f, a, r = step(m, ckb.h)
+            ck_ms.append(f + a + r)
+        ckd = float(np.mean(ck_ms))
+        t = ckb.tables_layout()
+        line["checkpointed_layout"] = {
+            "value": world * NF / (ckd * 1e-3), "unit": UNIT, "ms_per_step": ckd,
+            "cost_vs_full_tables": ckd / dev_step, "device_bytes": ckb.device_bytes,
+            "tables_held_bytes": 8 * t[3], "tables_full_bytes": 8 * t[2],
+            "what": "every size class recomputes each height level's tables before the adjoint walks it"}
+        ck_per = per_b.copy()
+        line["checkpointed_layout"]["max_rel_logl_vs_full_tables"] = float(np.max(np.where(
+            np.isneginf(ck_per) & np.isneginf(parity_per), 0.0,
+            np.abs(ck_per - parity_per) / np.maximum(np.abs(parity_per), 1e-300))))
+        del ckb
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         idx = pick_cpu_sample(W, wl, args.cpu_budget / 2, threads)

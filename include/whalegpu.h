@@ -60,6 +60,16 @@ extern "C" {
 /* Every task keeps its working rows in device memory, as the tasks too wide
  * for shared memory always do (a testing aid for that path; slower). */
 #define WG_BATCH_SCRATCH_ROWS 4u
+/* Per-branch checkpoint/recompute of the adjoint's DP tables in every size
+ * class: only the children's top rows are kept through the evaluation and
+ * each species-tree height level's tables are recomputed just before the
+ * adjoint walks that level, so the device holds one level's tables at a
+ * time.  Without this flag a gradient batch does this by itself for its
+ * largest size classes when storing every table would exceed the table
+ * budget (WG_TABLE_BUDGET_BYTES in the environment, else the device memory
+ * free at creation less the batch's other buffers and a 1 GiB reserve).
+ * Ignored with WG_BATCH_TABLES (logpdf! returns every table). */
+#define WG_BATCH_CHECKPOINT 8u
 
 typedef struct wg_ctx wg_ctx;
 typedef struct wg_model wg_model;
@@ -157,6 +167,13 @@ int wg_batch_info(const wg_batch* b, int32_t* n_families, int32_t* n_groups, int
 int wg_nowhere_condition(wg_ctx* ctx, const wg_model* m, double* value, double* d_lam, double* d_mu, double* d_q,
                          double* d_eta);
 
+/* Table layout of a gradient batch: size classes, how many of them recompute
+ * their tables per level (WG_BATCH_CHECKPOINT), the doubles every table
+ * would take and the doubles the device holds for tables.  Not in the
+ * reference (its tables are allocated per call, src/core.jl:41). */
+int wg_batch_tables_layout(const wg_batch* b, int32_t* classes, int32_t* checkpointed, int64_t* full_doubles,
+                           int64_t* kept_doubles);
+
 /* Kernel launches in one evaluation of the batch as last recorded: forward
  * only, and forward + adjoint + gradient reduction (0 before the first call
  * of that kind).  Not in the reference (a measurement aid). */
@@ -164,8 +181,9 @@ int wg_batch_launches(const wg_batch* b, int32_t* forward, int32_t* gradient);
 
 /* Pack a batch on the host only (no device needed) and report its layout:
  * tasks (CTAs over all launches), program entries, DP-table doubles kept for
- * the adjoint, largest shared memory per CTA (bytes) and the algorithmic
- * forward FLOPs. */
+ * the adjoint (with WG_BATCH_GRAD | WG_BATCH_CHECKPOINT: the one-level region
+ * of the per-level recomputation), largest shared memory per CTA (bytes) and
+ * the algorithmic forward FLOPs.  All families form one size class here. */
 int wg_pack_info(const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_t flags, int64_t* n_groups,
                  int64_t* n_entries, int64_t* table_doubles, int64_t* smem_bytes, double* flops_fwd);
 

@@ -17,7 +17,7 @@ WG_OK = 0
 WG_EINVAL, WG_EPARSE, WG_ECUDA, WG_ENOMEM, WG_ESTATE, WG_ERANGE = -1, -2, -3, -4, -5, -6
 NODE_LEAF, NODE_INTERNAL, NODE_WGD, NODE_ROOT = 0, 1, 2, 3
 COND_NONE, COND_ROOT, COND_NONEXTINCT, COND_NOWHERE = 0, 1, 2, 3
-BATCH_GRAD, BATCH_TABLES, BATCH_SCRATCH_ROWS = 1, 2, 4
+BATCH_GRAD, BATCH_TABLES, BATCH_SCRATCH_ROWS, BATCH_CHECKPOINT = 1, 2, 4, 8
 SYNTH_WALK, SYNTH_PUSH = 1, 2
 
 _ERRNAMES = {WG_EINVAL: "EINVAL", WG_EPARSE: "EPARSE", WG_ECUDA: "ECUDA", WG_ENOMEM: "ENOMEM",
@@ -75,6 +75,7 @@ def _declare(L):
         "wg_pack_tasks": (C.c_int, [vp, P_vp, i32, u32, P_i32, i64, P_i64]),
         "wg_batch_info": (C.c_int, [vp, P_i32, P_i32, P_i64, P_dbl, P_dbl, P_dbl]),
         "wg_batch_launches": (C.c_int, [vp, P_i32, P_i32]),
+        "wg_batch_tables_layout": (C.c_int, [vp, P_i32, P_i32, P_i64, P_i64]),
         "wg_nowhere_condition": (C.c_int, [vp, vp, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl]),
         "wg_backtrack": (C.c_int, [vp, vp, vp, C.c_int32, C.c_int32, C.c_uint64, C.c_char_p, C.c_int64, P_i64]),
         "wg_backtrack_tables": (C.c_int, [vp, vp, P_dbl, C.c_int64, C.c_int32, C.c_uint64, C.c_char_p, C.c_int64,

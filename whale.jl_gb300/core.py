@@ -84,14 +84,18 @@ class Batch:
     """Device-resident packed families (wg_batch) for one model structure."""
 
     def __init__(self, wm: WhaleModel, ccds: Sequence[CCD], grad: bool = False, tables: bool = False,
-                 ctx: Context = None, scratch_rows: bool = False):
+                 ctx: Context = None, scratch_rows: bool = False, checkpoint: bool = False):
         """scratch_rows: every task keeps its working rows in device memory,
-        as tasks too wide for shared memory always do (testing aid)."""
+        as tasks too wide for shared memory always do (testing aid).
+        checkpoint: the adjoint recomputes each height level's DP tables from
+        the children's top rows instead of keeping every table (a gradient
+        batch does this by itself for its largest size classes when the
+        tables would exceed the device-memory budget)."""
         self.ctx = ctx or default_context()
         self.ccds = list(ccds)
         self.n = len(self.ccds)
         flags = ((N.BATCH_GRAD if grad else 0) | (N.BATCH_TABLES if tables else 0)
-                 | (N.BATCH_SCRATCH_ROWS if scratch_rows else 0))
+                 | (N.BATCH_SCRATCH_ROWS if scratch_rows else 0) | (N.BATCH_CHECKPOINT if checkpoint else 0))
         arr = (N.C.c_void_p * self.n)(*[c._h for c in self.ccds])
         h = N.vp()
         N.check(N.lib().wg_batch_create(self.ctx.h, wm._struct.h, arr, self.n, flags, N.C.byref(h)))
@@ -106,6 +110,15 @@ class Batch:
                                       N.C.byref(fb), N.C.byref(fa)))
         self.n_groups, self.device_bytes = ng.value, by.value
         self.flops_fwd, self.bytes_fwd, self.flops_adj = ff.value, fb.value, fa.value
+
+    def tables_layout(self):
+        """(size classes, classes recomputing their tables per level, doubles
+        every table would take, doubles of tables held on the device)."""
+        c, k = N.i32(), N.i32()
+        full, kept = N.i64(), N.i64()
+        N.check(N.lib().wg_batch_tables_layout(self.h, N.C.byref(c), N.C.byref(k), N.C.byref(full),
+                                               N.C.byref(kept)))
+        return c.value, k.value, full.value, kept.value
 
     def __del__(self):
         if getattr(self, "h", None) and N._lib is not None:

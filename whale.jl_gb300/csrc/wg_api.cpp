@@ -297,6 +297,8 @@ int wg_pack_info(const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_
     opt.adjoint = (flags & WG_BATCH_GRAD) != 0;
     opt.keep_tables = (flags & (WG_BATCH_GRAD | WG_BATCH_TABLES)) != 0;
     wg::Packed2 P = wg::pack_batch2(*m, cs, opt);
+    // the per-level table region of a checkpointed gradient layout
+    if ((flags & WG_BATCH_CHECKPOINT) && opt.adjoint && !(flags & WG_BATCH_TABLES)) wg::checkpoint_tables(P, *m);
     if (n_groups) *n_groups = (int64_t)P.tasks.size();
     if (n_entries) *n_entries = (int64_t)P.entries.size();
     if (table_doubles) *table_doubles = P.tab_doubles;
@@ -317,10 +319,9 @@ int wg_pack_tasks(const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32
     *n_tasks = (int64_t)P.tasks.size();
     if (!out) return WG_OK;
     std::vector<int> level(P.tasks.size(), 0);
-    for (size_t L = 0; L < P.levels.size(); ++L) {
-      for (int t : P.levels[L]) level[t] = (int)L;
-      for (int t : P.levels_h[L]) level[t] = (int)L;
-    }
+    for (size_t L = 0; L < P.levels.size(); ++L)
+      for (const auto* lv : {&P.levels[L], &P.levels_h[L], &P.levels_g[L], &P.levels_gh[L]})
+        for (int t : *lv) level[t] = (int)L;
     for (size_t t = 0; t < P.tasks.size() && (int64_t)(t + 1) * 12 <= cap; ++t) {
       const wg::DTask& T = P.tasks[t];
       int32_t* o = out + 12 * t;

@@ -356,6 +356,11 @@ struct PackOptions2 {
 
 Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const PackOptions2& opt);
 
+// Re-lays a gradient layout's tables for per-level recomputation (every
+// height level's tasks share one region from offset 0); returns the doubles
+// that region needs.
+int64_t checkpoint_tables(Packed2& P, const Model& m);
+
 // For every node (model order) and clade: the clade's column among the
 // node's compatible clades (ascending clade id), -1 if incompatible.
 std::vector<std::vector<int>> compat_columns(const Model& m, const CCD& c);

@@ -1370,6 +1370,7 @@ struct SubBatch {
   double* d_gred = nullptr;
   int64_t gout_doubles = 0;
   int64_t tops_doubles = 0;
+  bool checkpoint = false;  // tables recomputed level by level in the adjoint (one level's tables held)
   cudaStream_t s = nullptr, s2 = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, done = nullptr;
   ~SubBatch() {
@@ -1389,6 +1390,8 @@ struct wg_batch {
   uint32_t flags = 0;
   int64_t device_bytes = 0;
   double flops_fwd = 0, bytes_fwd = 0, flops_adj = 0;
+  int64_t tab_full = 0, tab_kept = 0;  // table doubles: every table / held on the device
+  int n_checkpointed = 0;              // size classes that recompute their tables per level
   std::vector<std::unique_ptr<SubBatch>> subs;
   std::vector<int> fam_sub, fam_local;
   std::vector<int> nrow;
@@ -1521,6 +1524,33 @@ KArgs plain_args(const PlainBatch* b) {
 // higher stream priorities, so their CTAs are dispatched first.
 constexpr int kClassBounds[] = {128, 256, 512, 1024, 1536, 1 << 30};
 
+// Device bytes of a packed class other than its tables.
+int64_t class_other_bytes(const Packed2& P, bool adjoint, int P_params) {
+  int64_t by = (int64_t)(P.tasks.size() * sizeof(DTask) + P.entries.size() * sizeof(DEntry) +
+                         P.meta.size() * sizeof(int32_t) + P.gmap.size() * sizeof(int64_t) +
+                         P.progs.size() * sizeof(DProg2) + P.tasks.size() * sizeof(int32_t));
+  by += 8 * (P.tops_doubles + P.scratch_doubles);
+  if (adjoint)
+    by += 8 * (P.tops_doubles + P.gout_doubles + P_params) +
+          (int64_t)(P.red_off.size() + P.red_idx.size()) * (int64_t)sizeof(int64_t);
+  return by;
+}
+
+// Table budget of a gradient batch: WG_TABLE_BUDGET_BYTES, else the device
+// memory free now less the batch's other buffers and a 1 GiB reserve.
+int64_t table_budget(int64_t other_bytes) {
+  const char* e = std::getenv("WG_TABLE_BUDGET_BYTES");
+  if (e && *e) {
+    char* end = nullptr;
+    const long long v = std::strtoll(e, &end, 10);
+    if (end == e || *end != '\0' || v < 0) throw Error(WG_EINVAL, "WG_TABLE_BUDGET_BYTES is not a byte count");
+    return (int64_t)v;
+  }
+  size_t fr = 0, tot = 0;
+  ck(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+  return (int64_t)fr - other_bytes - ((int64_t)1 << 30);
+}
+
 std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* const* ccds, int n, uint32_t flags) {
   ck(cudaSetDevice(ctx->device), "cudaSetDevice");
   for (int i = 0; i < n; ++i)
@@ -1539,9 +1569,15 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
   int64_t& by = b->device_bytes;
   const bool adjoint = (flags & WG_BATCH_GRAD) != 0;
   const bool keep = (flags & (WG_BATCH_GRAD | WG_BATCH_TABLES)) != 0;
+  // ---- pack every size class on the host
+  struct Cls {
+    int cls;
+    std::vector<int> ids;
+    Packed2 P;
+    bool checkpoint = false;
+  };
+  std::vector<Cls> cl;
   int lo = 0;
-  int prio_lo = 0, prio_hi = 0;
-  ck(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi), "priority range");
   int cls = -1;
   for (int bound : kClassBounds) {
     ++cls;
@@ -1557,11 +1593,55 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
     opt.keep_tables = keep;
     opt.global_ids = &ids;
     opt.smem_limit_doubles = (flags & WG_BATCH_SCRATCH_ROWS) ? 0 : (int64_t)(ctx->smem_optin / sizeof(double));
-    Packed2 P = pack_batch2(*m, cs, opt);
-    if ((size_t)P.max_smem * sizeof(double) > ctx->smem_optin)
+    Cls c;
+    c.cls = cls;
+    c.P = pack_batch2(*m, cs, opt);
+    c.ids = std::move(ids);
+    if ((size_t)c.P.max_smem * sizeof(double) > ctx->smem_optin)
       throw Error(WG_ERANGE, "a task needs more shared memory than one CTA can hold");
+    cl.push_back(std::move(c));
+  }
+  // ---- per-branch checkpoint/recompute where the tables would not fit
+  b->tab_full = 0;
+  for (auto& c : cl) b->tab_full += c.P.tab_doubles;
+  if (adjoint && !(flags & WG_BATCH_TABLES)) {
+    if (flags & WG_BATCH_CHECKPOINT) {
+      for (auto& c : cl) {
+        c.checkpoint = true;
+        checkpoint_tables(c.P, *m);
+      }
+    } else {
+      int64_t other = 0, tabs = 0;
+      for (auto& c : cl) {
+        other += class_other_bytes(c.P, adjoint, b->P);
+        tabs += 8 * c.P.tab_doubles;
+      }
+      const int64_t budget = table_budget(other);
+      if (tabs > budget) {
+        // largest tables first, until the rest fit
+        std::vector<size_t> order(cl.size());
+        for (size_t i = 0; i < cl.size(); ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](size_t x, size_t y) { return cl[x].P.tab_doubles > cl[y].P.tab_doubles; });
+        for (size_t i : order) {
+          if (tabs <= budget) break;
+          Cls& c = cl[i];
+          const int64_t full = c.P.tab_doubles;
+          c.checkpoint = true;
+          const int64_t kept = checkpoint_tables(c.P, *m);
+          tabs -= 8 * (full - kept);
+        }
+      }
+    }
+  }
+  int prio_lo = 0, prio_hi = 0;
+  ck(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi), "priority range");
+  for (auto& c : cl) {
+    Packed2& P = c.P;
+    const std::vector<int>& ids = c.ids;
     auto sb = std::make_unique<SubBatch>();
     sb->device = ctx->device;
+    sb->checkpoint = c.checkpoint;
     sb->fam = ids;
     sb->n_tasks = (int)P.tasks.size();
     sb->fam_tab = P.fam_tab;
@@ -1572,6 +1652,8 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
     b->flops_fwd += P.flops_fwd;
     b->bytes_fwd += P.bytes_fwd;
     b->flops_adj += P.flops_adj;
+    b->tab_kept += P.tab_doubles;
+    if (c.checkpoint) ++b->n_checkpointed;
     for (size_t i = 0; i < ids.size(); ++i) {
       b->fam_sub[ids[i]] = (int)b->subs.size();
       b->fam_local[ids[i]] = (int)i;
@@ -1630,12 +1712,17 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
     h2d(sb->d_lists, lists, s);
     {
       // priority grows (numerically falls) with the class
-      const int pr = std::max(prio_hi, prio_lo - cls);
+      const int pr = std::max(prio_hi, prio_lo - c.cls);
       ck(cudaStreamCreateWithPriority(&sb->s, cudaStreamNonBlocking, pr), "cudaStreamCreate");
       ck(cudaStreamCreateWithPriority(&sb->s2, cudaStreamNonBlocking, pr), "cudaStreamCreate");
     }
     for (cudaEvent_t* e : {&sb->fork, &sb->join, &sb->done})
       ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
+    // the host copy of this class is no longer needed once its uploads landed
+    ck(cudaStreamSynchronize(s), "batch upload");
+    std::vector<DTask>().swap(P.tasks);
+    decltype(P.entries)().swap(P.entries);
+    std::vector<int64_t>().swap(P.gmap);
     b->subs.push_back(std::move(sb));
   }
   b->d_params = dalloc<double>(b->P + 2, by);
@@ -1758,51 +1845,56 @@ void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted, bool no
   if (grad)
     for (auto& sb : b->subs)
       ck(cudaMemsetAsync(sb->d_gout, 0, sizeof(double) * (size_t)sb->gout_doubles, s), "memset");
+  // the forward launches of one height level of one class; tab: the tasks
+  // store their DP tables
+  auto fwd_level = [&](SubBatch* sb, const KArgs2& A, int L, bool tab) {
+    const int top = (int)sb->lvl_n.size() - 1;  // the root level
+    const int* ll = sb->d_lists + sb->lvl_off[L];
+    const int* lh = sb->d_lists + sb->lvlh_off[L];
+    run_level(
+        sb, L,
+        [&](cudaStream_t st) {
+          const dim3 g(sb->lvl_n[L]), gg(sb->lvlg_n[L]);
+          const size_t sm = sb->lvl_smem[L];
+          const int* lg = sb->d_lists + sb->lvlg_off[L];
+          if (sb->lvl_n[L] > 0) {
+            ++nl;
+            if (L == top && tab) k_fwd2<true, kNT2L, true><<<g, kNT2L, sm, st>>>(A, ll);
+            else if (L == top) k_fwd2<false, kNT2L, true><<<g, kNT2L, sm, st>>>(A, ll);
+            else if (tab) k_fwd2<true, kNT2L><<<g, kNT2L, sm, st>>>(A, ll);
+            else k_fwd2<false, kNT2L><<<g, kNT2L, sm, st>>>(A, ll);
+          }
+          if (sb->lvlg_n[L] > 0) {
+            ++nl;
+            if (L == top && tab) k_fwd2<true, kNT2L, true, true><<<gg, kNT2L, 0, st>>>(A, lg);
+            else if (L == top) k_fwd2<false, kNT2L, true, true><<<gg, kNT2L, 0, st>>>(A, lg);
+            else if (tab) k_fwd2<true, kNT2L, false, true><<<gg, kNT2L, 0, st>>>(A, lg);
+            else k_fwd2<false, kNT2L, false, true><<<gg, kNT2L, 0, st>>>(A, lg);
+          }
+        },
+        [&](cudaStream_t st) {
+          const int* lgh = sb->d_lists + sb->lvlgh_off[L];
+          if (sb->lvlh_n[L] > 0) {
+            ++nl;
+            if (tab) k_fwd2<true, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], st>>>(A, lh);
+            else k_fwd2<false, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], st>>>(A, lh);
+          }
+          if (sb->lvlgh_n[L] > 0) {
+            ++nl;
+            if (tab) k_fwd2<true, kNT2H, false, true><<<sb->lvlgh_n[L], kNT2H, 0, st>>>(A, lgh);
+            else k_fwd2<false, kNT2H, false, true><<<sb->lvlgh_n[L], kNT2H, 0, st>>>(A, lgh);
+          }
+        });
+  };
   ck(cudaEventRecordWithFlags(ctx->ev[0], s, cudaEventRecordExternal), "event");
   fork_subs(b);
   for (auto& sbp : b->subs) {
     SubBatch* sb = sbp.get();
     KArgs2 A = sub_args(b, sb);
     A.famw = weighted ? b->d_famw : nullptr;
-    const int top = (int)sb->lvl_n.size() - 1;  // the root level
-    for (int L = 0; L < (int)sb->lvl_n.size(); ++L) {
-      const int* ll = sb->d_lists + sb->lvl_off[L];
-      const int* lh = sb->d_lists + sb->lvlh_off[L];
-      run_level(
-          sb, L,
-          [&](cudaStream_t st) {
-            const dim3 g(sb->lvl_n[L]), gg(sb->lvlg_n[L]);
-            const size_t sm = sb->lvl_smem[L];
-            const int* lg = sb->d_lists + sb->lvlg_off[L];
-            if (sb->lvl_n[L] > 0) {
-              ++nl;
-              if (L == top && tables) k_fwd2<true, kNT2L, true><<<g, kNT2L, sm, st>>>(A, ll);
-              else if (L == top) k_fwd2<false, kNT2L, true><<<g, kNT2L, sm, st>>>(A, ll);
-              else if (tables) k_fwd2<true, kNT2L><<<g, kNT2L, sm, st>>>(A, ll);
-              else k_fwd2<false, kNT2L><<<g, kNT2L, sm, st>>>(A, ll);
-            }
-            if (sb->lvlg_n[L] > 0) {
-              ++nl;
-              if (L == top && tables) k_fwd2<true, kNT2L, true, true><<<gg, kNT2L, 0, st>>>(A, lg);
-              else if (L == top) k_fwd2<false, kNT2L, true, true><<<gg, kNT2L, 0, st>>>(A, lg);
-              else if (tables) k_fwd2<true, kNT2L, false, true><<<gg, kNT2L, 0, st>>>(A, lg);
-              else k_fwd2<false, kNT2L, false, true><<<gg, kNT2L, 0, st>>>(A, lg);
-            }
-          },
-          [&](cudaStream_t st) {
-            const int* lgh = sb->d_lists + sb->lvlgh_off[L];
-            if (sb->lvlh_n[L] > 0) {
-              ++nl;
-              if (tables) k_fwd2<true, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], st>>>(A, lh);
-              else k_fwd2<false, kNT2H><<<sb->lvlh_n[L], kNT2H, sb->lvlh_smem[L], st>>>(A, lh);
-            }
-            if (sb->lvlgh_n[L] > 0) {
-              ++nl;
-              if (tables) k_fwd2<true, kNT2H, false, true><<<sb->lvlgh_n[L], kNT2H, 0, st>>>(A, lgh);
-              else k_fwd2<false, kNT2H, false, true><<<sb->lvlgh_n[L], kNT2H, 0, st>>>(A, lgh);
-            }
-          });
-    }
+    // a checkpointed class keeps no tables in the forward: its adjoint
+    // recomputes them level by level
+    for (int L = 0; L < (int)sb->lvl_n.size(); ++L) fwd_level(sb, A, L, tables && !sb->checkpoint);
   }
   ck(cudaGetLastError(), "forward launch");
   join_subs(b);
@@ -1818,6 +1910,9 @@ void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted, bool no
       for (int L = (int)sb->lvl_n.size() - 1; L >= 0; --L) {
         const int* ll = sb->d_lists + sb->lvl_off[L];
         const int* lh = sb->d_lists + sb->lvlh_off[L];
+        // checkpointed class: this level's tables again, from the children's
+        // top rows, into the region the level above has finished with
+        if (sb->checkpoint) fwd_level(sb, A, L, true);
         run_level(
             sb, L,
             [&](cudaStream_t st) {
@@ -2207,6 +2302,17 @@ int wg_nowhere_condition(wg_ctx* ctx, const wg_model* m, double* value, double* 
       if (d_q) d_q[k] = r.ok ? r.d_q[k] : 0.0;
     }
     if (d_eta) *d_eta = r.ok ? r.d_eta : 0.0;
+  });
+}
+
+int wg_batch_tables_layout(const wg_batch* b, int32_t* classes, int32_t* checkpointed, int64_t* full_doubles,
+                           int64_t* kept_doubles) {
+  WG_GUARD({
+    if (!b) throw Error(WG_EINVAL, "null batch");
+    if (classes) *classes = (int32_t)b->subs.size();
+    if (checkpointed) *checkpointed = b->n_checkpointed;
+    if (full_doubles) *full_doubles = b->tab_full;
+    if (kept_doubles) *kept_doubles = b->tab_kept;
   });
 }
 

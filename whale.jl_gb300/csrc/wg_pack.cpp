@@ -1180,4 +1180,27 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
   return P;
 }
 
+// Checkpointed tables: the adjoint recomputes each height level's tables from
+// the children's top rows (kept in the tops buffer for the whole evaluation,
+// one row per species branch and family) just before it walks that level, so
+// only one level's tables exist at a time.  Every level's tasks take table
+// offsets from 0; the region is the largest level's.  Family table offsets
+// are dropped: no family's tables outlive its level.
+int64_t checkpoint_tables(Packed2& P, const Model& m) {
+  int64_t need = 0;
+  for (size_t h = 0; h < P.levels.size(); ++h) {
+    int64_t off = 0;
+    for (const auto* lv : {&P.levels[h], &P.levels_h[h], &P.levels_g[h], &P.levels_gh[h]})
+      for (int t : *lv) {
+        DTask& T = P.tasks[t];
+        T.tab = off;
+        off += (int64_t)m.nrow[T.node] * T.width;
+      }
+    need = std::max(need, off);
+  }
+  std::fill(P.fam_tab.begin(), P.fam_tab.end(), (int64_t)-1);
+  P.tab_doubles = need;
+  return need;
+}
+
 }  // namespace wg
