@@ -70,6 +70,12 @@ extern "C" {
  * free at creation less the batch's other buffers and a 1 GiB reserve).
  * Ignored with WG_BATCH_TABLES (logpdf! returns every table). */
 #define WG_BATCH_CHECKPOINT 8u
+/* One persistent launch per pass (forward, adjoint) over every task of the
+ * batch instead of one launch per species-tree height level and size class:
+ * CTAs take tasks in a topological order and wait (bounded) for the tasks
+ * whose rows they read.  A wait that runs out of polls makes the call return
+ * WG_ECUDA.  Not with WG_BATCH_CHECKPOINT (that layout keeps level launches). */
+#define WG_BATCH_PERSISTENT 16u
 
 typedef struct wg_ctx wg_ctx;
 typedef struct wg_model wg_model;
@@ -183,7 +189,9 @@ int wg_batch_launches(const wg_batch* b, int32_t* forward, int32_t* gradient);
  * tasks (CTAs over all launches), program entries, DP-table doubles kept for
  * the adjoint (with WG_BATCH_GRAD | WG_BATCH_CHECKPOINT: the one-level region
  * of the per-level recomputation), largest shared memory per CTA (bytes) and
- * the algorithmic forward FLOPs.  All families form one size class here. */
+ * the algorithmic forward FLOPs.  All families form one size class here.
+ * With WG_BATCH_PERSISTENT the layout (and its persistent schedule, which is
+ * checked) is packed as that flag packs it. */
 int wg_pack_info(const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_t flags, int64_t* n_groups,
                  int64_t* n_entries, int64_t* table_doubles, int64_t* smem_bytes, double* flops_fwd);
 

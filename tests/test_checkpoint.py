@@ -42,3 +42,17 @@ def test_checkpoint_layout_holds_one_level(W):
     # logpdf! keeps every table: the flag does not apply with WG_BATCH_TABLES
     both, _ = _pack(W, wm, ccds, N.BATCH_GRAD | N.BATCH_TABLES | N.BATCH_CHECKPOINT)
     assert both == full
+
+
+def test_persistent_layout_schedule(W):
+    # the persistent layout packs every task for 128 threads and builds its
+    # ticket orders and dependency lists (checked topological on the host)
+    from whale_gb300 import _native as N
+    from whale_gb300 import synth
+
+    for wl in (synth.config1(n_families=300), synth.config0(n_families=50)):
+        wm, ccds = wl.model, wl.ccds()
+        tab, tasks = _pack(W, wm, ccds, N.BATCH_GRAD | N.BATCH_PERSISTENT)
+        assert np.all(tasks[:, 5] <= 128) and np.all(tasks[:, 9] <= 128)
+        full, _ = _pack(W, wm, ccds, N.BATCH_GRAD)
+        assert tab > 0 and full > 0

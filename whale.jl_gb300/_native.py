@@ -17,7 +17,7 @@ WG_OK = 0
 WG_EINVAL, WG_EPARSE, WG_ECUDA, WG_ENOMEM, WG_ESTATE, WG_ERANGE = -1, -2, -3, -4, -5, -6
 NODE_LEAF, NODE_INTERNAL, NODE_WGD, NODE_ROOT = 0, 1, 2, 3
 COND_NONE, COND_ROOT, COND_NONEXTINCT, COND_NOWHERE = 0, 1, 2, 3
-BATCH_GRAD, BATCH_TABLES, BATCH_SCRATCH_ROWS, BATCH_CHECKPOINT = 1, 2, 4, 8
+BATCH_GRAD, BATCH_TABLES, BATCH_SCRATCH_ROWS, BATCH_CHECKPOINT, BATCH_PERSISTENT = 1, 2, 4, 8, 16
 SYNTH_WALK, SYNTH_PUSH = 1, 2
 
 _ERRNAMES = {WG_EINVAL: "EINVAL", WG_EPARSE: "EPARSE", WG_ECUDA: "ECUDA", WG_ENOMEM: "ENOMEM",

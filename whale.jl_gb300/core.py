@@ -84,18 +84,22 @@ class Batch:
     """Device-resident packed families (wg_batch) for one model structure."""
 
     def __init__(self, wm: WhaleModel, ccds: Sequence[CCD], grad: bool = False, tables: bool = False,
-                 ctx: Context = None, scratch_rows: bool = False, checkpoint: bool = False):
+                 ctx: Context = None, scratch_rows: bool = False, checkpoint: bool = False,
+                 persistent: bool = False):
         """scratch_rows: every task keeps its working rows in device memory,
         as tasks too wide for shared memory always do (testing aid).
         checkpoint: the adjoint recomputes each height level's DP tables from
         the children's top rows instead of keeping every table (a gradient
         batch does this by itself for its largest size classes when the
-        tables would exceed the device-memory budget)."""
+        tables would exceed the device-memory budget).
+        persistent: one persistent launch per pass over every task, CTAs
+        taking tasks in a topological order (bounded dependency waits)."""
         self.ctx = ctx or default_context()
         self.ccds = list(ccds)
         self.n = len(self.ccds)
         flags = ((N.BATCH_GRAD if grad else 0) | (N.BATCH_TABLES if tables else 0)
-                 | (N.BATCH_SCRATCH_ROWS if scratch_rows else 0) | (N.BATCH_CHECKPOINT if checkpoint else 0))
+                 | (N.BATCH_SCRATCH_ROWS if scratch_rows else 0) | (N.BATCH_CHECKPOINT if checkpoint else 0)
+                 | (N.BATCH_PERSISTENT if persistent else 0))
         arr = (N.C.c_void_p * self.n)(*[c._h for c in self.ccds])
         h = N.vp()
         N.check(N.lib().wg_batch_create(self.ctx.h, wm._struct.h, arr, self.n, flags, N.C.byref(h)))

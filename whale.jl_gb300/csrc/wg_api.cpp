@@ -288,15 +288,30 @@ int wg_ccd_export(const wg_ccd* c, int32_t* nleaves, int64_t* counts, int32_t* s
   });
 }
 
+// Packing options of a batch with these flags, as wg_batch_create sets them
+// for a device with 227 KB of shared memory per CTA (one size class).
+static wg::PackOptions2 host_pack_options(uint32_t flags) {
+  wg::PackOptions2 opt;
+  opt.adjoint = (flags & WG_BATCH_GRAD) != 0;
+  opt.keep_tables = (flags & (WG_BATCH_GRAD | WG_BATCH_TABLES)) != 0;
+  if (flags & WG_BATCH_PERSISTENT) {
+    const int64_t cap = 227 * 1024 / 8 / wg::pack_knob("WG_PERSIST_CTAS", 3, 1, 8) - 64;
+    opt.light_only = true;
+    opt.root_smem_doubles = cap;
+    opt.smem_limit_doubles = cap;
+  }
+  return opt;
+}
+
 int wg_pack_info(const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_t flags, int64_t* n_groups,
                  int64_t* n_entries, int64_t* table_doubles, int64_t* smem_bytes, double* flops_fwd) {
   WG_GUARD({
     if (!m || !ccds || n_ccds <= 0) throw wg::Error(WG_EINVAL, "wg_pack_info: bad arguments");
     std::vector<const wg::CCD*> cs(ccds, ccds + n_ccds);
-    wg::PackOptions2 opt;
-    opt.adjoint = (flags & WG_BATCH_GRAD) != 0;
-    opt.keep_tables = (flags & (WG_BATCH_GRAD | WG_BATCH_TABLES)) != 0;
+    const wg::PackOptions2 opt = host_pack_options(flags);
     wg::Packed2 P = wg::pack_batch2(*m, cs, opt);
+    // the persistent schedule is checked here too (topological ticket orders)
+    if (flags & WG_BATCH_PERSISTENT) (void)wg::persistent_schedule(P);
     // the per-level table region of a checkpointed gradient layout
     if ((flags & WG_BATCH_CHECKPOINT) && opt.adjoint && !(flags & WG_BATCH_TABLES)) wg::checkpoint_tables(P, *m);
     if (n_groups) *n_groups = (int64_t)P.tasks.size();
@@ -312,10 +327,7 @@ int wg_pack_tasks(const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32
   WG_GUARD({
     if (!m || !ccds || n_ccds <= 0 || !n_tasks) throw wg::Error(WG_EINVAL, "wg_pack_tasks: bad arguments");
     std::vector<const wg::CCD*> cs(ccds, ccds + n_ccds);
-    wg::PackOptions2 opt;
-    opt.adjoint = (flags & WG_BATCH_GRAD) != 0;
-    opt.keep_tables = (flags & (WG_BATCH_GRAD | WG_BATCH_TABLES)) != 0;
-    wg::Packed2 P = wg::pack_batch2(*m, cs, opt);
+    wg::Packed2 P = wg::pack_batch2(*m, cs, host_pack_options(flags));
     *n_tasks = (int64_t)P.tasks.size();
     if (!out) return WG_OK;
     std::vector<int> level(P.tasks.size(), 0);

@@ -348,6 +348,11 @@ struct PackOptions2 {
   // device memory (L2-resident) instead
   int64_t smem_limit_doubles = 227 * 1024 / 8;
   int target_j = (int)pack_knob("WG_PACK_TARGET_J", 3, 1, 16);  // iterations per row the lane scheduler aims for
+  // persistent launches: every task takes kNT2L threads, and a root task's
+  // families are grouped so that its adjoint rows fit in this many shared
+  // doubles (0: no such bound)
+  bool light_only = false;
+  int64_t root_smem_doubles = 0;
   bool keep_tables = false;
   bool adjoint = false;
   const std::vector<int>* global_ids = nullptr;  // family index written to log L outputs
@@ -355,6 +360,18 @@ struct PackOptions2 {
 };
 
 Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const PackOptions2& opt);
+
+// Schedule of a layout run as one persistent launch per pass: the tickets'
+// task order of the forward (height levels upwards, each level in launch
+// order) and of the adjoint (levels downwards), and per task the tasks it
+// waits for: in the forward the producers of the children's top rows it
+// stages, in the adjoint the tasks that stage its own top row (they write its
+// top-row adjoints).  CSR, task indices of the layout.
+struct Schedule {
+  std::vector<int32_t> order_fwd, order_adj;
+  std::vector<int32_t> fdep_off, fdep_idx, adep_off, adep_idx;
+};
+Schedule persistent_schedule(const Packed2& P);
 
 // Re-lays a gradient layout's tables for per-level recomputation (every
 // height level's tasks share one region from offset 0); returns the doubles

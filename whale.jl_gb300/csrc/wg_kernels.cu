@@ -606,23 +606,27 @@ __device__ __forceinline__ bool fwd_rows_dispatch(int j, const DEntry* __restric
   }
 }
 
-// ROOT: the launch of the top level, whose tasks are all root tasks; the other
-// launches hold no root task.  Separate instantiations keep the root-row
-// machinery out of the register budget of the branch kernels.
-// GLOBAL: the tasks of the launch keep their working rows in device memory
-// (A.scratch + T.scratch, L2-resident) because they do not fit in shared
-// memory; the code is otherwise the same.
-template <bool TABLES, int NT, bool ROOT = false, bool GLOBAL = false>
-__global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restrict__ list) {
-  extern __shared__ double smem_dyn[];
-  const DTask& T = A.tasks[list[blockIdx.x]];
+// Top rows (forward) and their adjoints (reverse) written by other CTAs of
+// the same launch are read through L2 only (ld.global.cg): the SM's L1 is not
+// coherent with other SMs' stores and may hold an older copy of the line.
+template <bool CG>
+__device__ __forceinline__ double ld_shared_row(const double* p) {
+  if constexpr (CG) return __ldcg(p);
+  else return *p;
+}
+
+// One forward task (one species node for a group of families).  rot rotates
+// the lane assignment by warps (spreads the lanes' programs over the warps of
+// successive CTAs); CG: the children's top rows were written in this launch.
+template <bool TABLES, int NT, bool ROOT, bool GLOBAL, bool CG>
+__device__ __forceinline__ void fwd_task(const KArgs2& A, const DTask& T, int rot, double* smem_dyn) {
   double* const sm = GLOBAL ? A.scratch + T.scratch : smem_dyn;
   const int k = T.node;
   const int4 mn = A.mnode[k];
   const int R = T.width;
   const int W2 = max(R, T.wa + T.wb);
   const int tid = threadIdx.x;
-  const int lane = (tid + 32 * (int)(blockIdx.x & (NT / 32 - 1))) & (NT - 1);
+  const int lane = (tid + 32 * (int)(rot & (NT / 32 - 1))) & (NT - 1);
   double* cur = sm;
   double* nxt = sm + W2;
   double* part = sm + 2 * W2;
@@ -645,7 +649,7 @@ __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restri
     for (int c = tid; c < R; c += NT) cur[c] = aux[c] ? lp : 0.0;
   } else {
     const int64_t* gm = A.gmap + T.gmap;
-    for (int i = tid; i < T.wa + T.wb; i += NT) nxt[i] = A.tops[gm[i]];
+    for (int i = tid; i < T.wa + T.wb; i += NT) nxt[i] = ld_shared_row<CG>(A.tops + gm[i]);
     __syncthreads();
     const double* X = nxt;
     const double* Y = nxt + T.wa;
@@ -710,6 +714,18 @@ __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restri
       A.logl[fp.x] = L > 0.0 ? log(L) : -INFINITY;
     }
   }
+}
+
+// ROOT: the launch of the top level, whose tasks are all root tasks; the other
+// launches hold no root task.  Separate instantiations keep the root-row
+// machinery out of the register budget of the branch kernels.
+// GLOBAL: the tasks of the launch keep their working rows in device memory
+// (A.scratch + T.scratch, L2-resident) because they do not fit in shared
+// memory; the code is otherwise the same.
+template <bool TABLES, int NT, bool ROOT = false, bool GLOBAL = false>
+__global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restrict__ list) {
+  extern __shared__ double smem_dyn[];
+  fwd_task<TABLES, NT, ROOT, GLOBAL, false>(A, A.tasks[list[blockIdx.x]], (int)blockIdx.x, smem_dyn);
 }
 
 // ---- adjoint helpers -------------------------------------------------------
@@ -1008,21 +1024,17 @@ __device__ __forceinline__ bool adj_rows_dispatch(int j, const DEntry* __restric
   }
 }
 
-// ROOT as for k_fwd2.  Four 128-thread CTAs per SM leave the adjoint its
-// ~110 registers: at five or six the spills cost more than the occupancy
-// gains (the rows are latency-bound, not FP64-bound).
-template <int NT, bool ROOT = false, bool GLOBAL = false>
-__global__ void __launch_bounds__(NT, NT == 128 && !GLOBAL ? 4 : (GLOBAL ? 1 : 2))
-    k_adj2(const KArgs2 A, const int* __restrict__ list) {
-  extern __shared__ double smem_dyn[];
-  const DTask& T = A.tasks[list[blockIdx.x]];
+// One adjoint task; rot and CG as for fwd_task (CG: the task's own top-row
+// adjoints were written by its parents' tasks in this launch).
+template <int NT, bool ROOT, bool GLOBAL, bool CG>
+__device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int rot, double* smem_dyn) {
   double* const sm = GLOBAL ? A.scratch + T.scratch : smem_dyn;
   const int k = T.node;
   const int4 mn = A.mnode[k];
   const int R = T.width;
   const int W2 = max(R, T.wa + T.wb);
   const int tid = threadIdx.x;
-  const int lane = (tid + 32 * (int)(blockIdx.x & (NT / 32 - 1))) & (NT - 1);
+  const int lane = (tid + 32 * (int)(rot & (NT / 32 - 1))) & (NT - 1);
   const int NR = A.NR;
   const int roff = A.row_off[k];
   const int n = mn.w;
@@ -1139,7 +1151,7 @@ __global__ void __launch_bounds__(NT, NT == 128 && !GLOBAL ? 4 : (GLOBAL ? 1 : 2
     return;
   }
   // ---- rows n-1 .. 1 of the branch (within_branch!)
-  for (int c = tid; c < R; c += NT) bar[c] = A.bartops[T.top + c];
+  for (int c = tid; c < R; c += NT) bar[c] = ld_shared_row<CG>(A.bartops + T.top + c);
   if (n > 1) {
     double* phs = red + 16 * (NT / 32);  // ϕ, ψ of this branch's rows
     double* pss = phs + n;
@@ -1230,6 +1242,16 @@ __global__ void __launch_bounds__(NT, NT == 128 && !GLOBAL ? 4 : (GLOBAL ? 1 : 2
   }
 }
 
+// ROOT as for k_fwd2.  Four 128-thread CTAs per SM leave the adjoint its
+// ~110 registers: at five or six the spills cost more than the occupancy
+// gains (the rows are latency-bound, not FP64-bound).
+template <int NT, bool ROOT = false, bool GLOBAL = false>
+__global__ void __launch_bounds__(NT, NT == 128 && !GLOBAL ? 4 : (GLOBAL ? 1 : 2))
+    k_adj2(const KArgs2 A, const int* __restrict__ list) {
+  extern __shared__ double smem_dyn[];
+  adj_task<NT, ROOT, GLOBAL, false>(A, A.tasks[list[blockIdx.x]], (int)blockIdx.x, smem_dyn);
+}
+
 // Gradient reduction: out[j] = Σ gout[idx] over the fixed contributor list of
 // j; one warp per output, lane-strided partial sums and a fixed butterfly.
 __global__ void k_reduce2(const double* __restrict__ gout, const int64_t* __restrict__ off,
@@ -1241,6 +1263,116 @@ __global__ void k_reduce2(const double* __restrict__ gout, const int64_t* __rest
   for (int64_t i = off[j] + lane; i < off[j + 1]; i += 32) s += gout[idx[i]];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) out[j] = s;
+}
+
+// ===========================================================================
+// Persistent launches: one kernel per pass over every task of a layout.
+// CTAs take tickets in a topological order of the pass (an atomic counter);
+// a task waits until the tasks it depends on have published their results,
+// runs, and publishes its own.  A task's dependencies hold earlier tickets,
+// so each is finished or held by a running CTA: the unfinished task with the
+// lowest ticket can always proceed and the waits cannot deadlock.  Every wait
+// is bounded: past the poll limit the CTA sets an error bit (which the host
+// turns into WG_ECUDA), skips the task's work and still publishes it, so the
+// launch ends in bounded time.
+// ===========================================================================
+struct PArgs {
+  const int* order;    // ticket -> task
+  const int* dep_off;  // per task: the tasks it waits for (CSR)
+  const int* dep_idx;
+  int* done;           // per task: 1 once published in this pass; [n] is never set
+  int* ticket;         // next ticket of this pass
+  int* err;            // bit 0: a dependency wait gave up
+  int n;
+  int spin_cap;        // polls per dependency before giving up
+  int wait_unset;      // test aid: every task also waits on done[n], which nothing sets
+};
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Bounded wait of one flag; false when the poll limit ran out.
+__device__ __forceinline__ bool wait_flag(const int* f, int cap) {
+  for (int polls = 0; ld_acquire_gpu(f) == 0; ++polls) {
+    if (polls >= cap) return false;
+    __nanosleep(200);
+  }
+  return true;
+}
+
+// Every thread waits for a share of the task's dependencies; true when all
+// were published (a CTA barrier orders the waits before the task's reads).
+__device__ __forceinline__ bool wait_deps(const PArgs& P, int task) {
+  bool ok = true;
+  const int b = P.dep_off[task], e = P.dep_off[task + 1];
+  for (int i = b + (int)threadIdx.x; i < e && ok; i += blockDim.x) ok = wait_flag(P.done + P.dep_idx[i], P.spin_cap);
+  if (P.wait_unset && threadIdx.x == 0) ok = ok && wait_flag(P.done + P.n, P.spin_cap);
+  const bool all = __syncthreads_and(ok) != 0;
+  if (!all && threadIdx.x == 0) atomicOr(P.err, 1);
+  return all;
+}
+
+// Publishes a finished task: the barrier orders every thread's stores before
+// thread 0's release.
+__device__ __forceinline__ void publish(const PArgs& P, int task) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    st_release_gpu(P.done + task, 1);
+  }
+}
+
+// Persistent forward: any task of the layout (root or branch, rows in shared
+// or device memory) with kNT2L threads; the dynamic shared memory is the
+// largest of the layout's shared-memory tasks.
+template <bool TABLES>
+__global__ void __launch_bounds__(kNT2L, 4) k_fwd_persist(const KArgs2 A, const PArgs P) {
+  extern __shared__ double smem_dyn[];
+  __shared__ int s_t;
+  for (;;) {
+    if (threadIdx.x == 0) s_t = atomicAdd(P.ticket, 1);
+    __syncthreads();
+    const int t = s_t;
+    if (t >= P.n) return;
+    const int task = P.order[t];
+    if (wait_deps(P, task)) {  // (its barrier also lets s_t be rewritten)
+      const DTask& T = A.tasks[task];
+      const bool root = A.mnode[T.node].x == WG_NODE_ROOT;
+      if (root && T.scratch >= 0) fwd_task<TABLES, kNT2L, true, true, true>(A, T, t, smem_dyn);
+      else if (root) fwd_task<TABLES, kNT2L, true, false, true>(A, T, t, smem_dyn);
+      else if (T.scratch >= 0) fwd_task<TABLES, kNT2L, false, true, true>(A, T, t, smem_dyn);
+      else fwd_task<TABLES, kNT2L, false, false, true>(A, T, t, smem_dyn);
+    }
+    publish(P, task);
+  }
+}
+
+// Persistent adjoint, tickets from the root level down.
+__global__ void __launch_bounds__(kNT2L, 4) k_adj_persist(const KArgs2 A, const PArgs P) {
+  extern __shared__ double smem_dyn[];
+  __shared__ int s_t;
+  for (;;) {
+    if (threadIdx.x == 0) s_t = atomicAdd(P.ticket, 1);
+    __syncthreads();
+    const int t = s_t;
+    if (t >= P.n) return;
+    const int task = P.order[t];
+    if (wait_deps(P, task)) {
+      const DTask& T = A.tasks[task];
+      const bool root = A.mnode[T.node].x == WG_NODE_ROOT;
+      if (root && T.scratch >= 0) adj_task<kNT2L, true, true, true>(A, T, t, smem_dyn);
+      else if (root) adj_task<kNT2L, true, false, true>(A, T, t, smem_dyn);
+      else if (T.scratch >= 0) adj_task<kNT2L, false, true, true>(A, T, t, smem_dyn);
+      else adj_task<kNT2L, false, false, true>(A, T, t, smem_dyn);
+    }
+    publish(P, task);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1371,11 +1503,21 @@ struct SubBatch {
   int64_t gout_doubles = 0;
   int64_t tops_doubles = 0;
   bool checkpoint = false;  // tables recomputed level by level in the adjoint (one level's tables held)
+  // persistent launches (one kernel per pass): ticket orders, dependency
+  // lists, per-task flags and the ticket / error counters
+  bool persist = false;
+  int n_pdep_f = 0, n_pdep_a = 0;
+  int* d_porder = nullptr;  // forward order (n_tasks) then adjoint order
+  int* d_pdep = nullptr;    // forward CSR (n_tasks + 1 offsets, indices) then adjoint CSR
+  int* d_pdone = nullptr;   // n_tasks + 1 flags
+  int* d_pctl = nullptr;    // [0] ticket, [1] error bits
+  size_t psmem_f = 0, psmem_a = 0;
+  int pgrid_f = 0, pgrid_a = 0;
   cudaStream_t s = nullptr, s2 = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, done = nullptr;
   ~SubBatch() {
     free_all(device, {d_tasks, d_entries, d_meta, d_gmap, d_progs, d_lists, d_red_off, d_red_idx, d_tops, d_tabs,
-                      d_bartops, d_gout, d_gred, d_scratch},
+                      d_bartops, d_gout, d_gred, d_scratch, d_porder, d_pdep, d_pdone, d_pctl},
              {});
     for (cudaEvent_t e : {fork, join, done})
       if (e) cudaEventDestroy(e);
@@ -1391,6 +1533,9 @@ struct wg_batch {
   int64_t device_bytes = 0;
   double flops_fwd = 0, bytes_fwd = 0, flops_adj = 0;
   int64_t tab_full = 0, tab_kept = 0;  // table doubles: every table / held on the device
+  bool persist = false;                // persistent launches (WG_BATCH_PERSISTENT)
+  int* h_perr = nullptr;               // error bits of the last evaluation's persistent passes (pinned)
+  int persist_spin_cap = 1 << 22, persist_wait_unset = 0;
   int n_checkpointed = 0;              // size classes that recompute their tables per level
   std::vector<std::unique_ptr<SubBatch>> subs;
   std::vector<int> fam_sub, fam_local;
@@ -1435,7 +1580,7 @@ struct wg_batch {
     if (ctx) free_all(ctx->device, {d_famw}, {h_famw});
     plain.reset();
     subs.clear();
-    if (ctx) free_all(ctx->device, {d_mnode, d_rowoff, d_leafp, d_params, d_logl}, {h_params, h_logl, h_gred});
+    if (ctx) free_all(ctx->device, {d_mnode, d_rowoff, d_leafp, d_params, d_logl}, {h_params, h_logl, h_gred, h_perr});
   }
 };
 
@@ -1579,7 +1724,19 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
   std::vector<Cls> cl;
   int lo = 0;
   int cls = -1;
-  for (int bound : kClassBounds) {
+  // persistent launches: one layout of 128-thread tasks whose shared memory
+  // fits WG_PERSIST_CTAS (default 3) CTAs per SM; wider tasks keep their rows
+  // in device memory
+  b->persist = (flags & WG_BATCH_PERSISTENT) != 0;
+  const int64_t pctas = pack_knob("WG_PERSIST_CTAS", 3, 1, 8);
+  const int64_t pcap = (int64_t)(ctx->smem_optin / (size_t)pctas) / (int64_t)sizeof(double) - 64;
+  b->persist_spin_cap = (int)pack_knob("WG_PERSIST_SPIN_CAP", 1 << 22, 0, 1 << 30);
+  b->persist_wait_unset = (int)pack_knob("WG_PERSIST_TEST_UNSET_WAIT", 0, 0, 1);
+  const int single_class[] = {1 << 30};
+  const int* bounds_begin = b->persist ? single_class : kClassBounds;
+  const int* bounds_end = b->persist ? single_class + 1 : kClassBounds + sizeof(kClassBounds) / sizeof(int);
+  for (const int* bp = bounds_begin; bp != bounds_end; ++bp) {
+    const int bound = *bp;
     ++cls;
     std::vector<int> ids;
     for (int i = 0; i < n; ++i)
@@ -1593,6 +1750,11 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
     opt.keep_tables = keep;
     opt.global_ids = &ids;
     opt.smem_limit_doubles = (flags & WG_BATCH_SCRATCH_ROWS) ? 0 : (int64_t)(ctx->smem_optin / sizeof(double));
+    if (b->persist) {
+      opt.light_only = true;
+      opt.root_smem_doubles = pcap;
+      if (!(flags & WG_BATCH_SCRATCH_ROWS)) opt.smem_limit_doubles = pcap;
+    }
     Cls c;
     c.cls = cls;
     c.P = pack_batch2(*m, cs, opt);
@@ -1710,6 +1872,43 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
     h2d(sb->d_gmap, P.gmap, s);
     h2d(sb->d_progs, P.progs, s);
     h2d(sb->d_lists, lists, s);
+    // persistent launches need every table kept (a checkpointed class keeps
+    // its level launches)
+    sb->persist = b->persist && !c.checkpoint;
+    if (sb->persist) {
+      const Schedule S = persistent_schedule(P);
+      const int nt = sb->n_tasks;
+      std::vector<int> ord(S.order_fwd.begin(), S.order_fwd.end());
+      ord.insert(ord.end(), S.order_adj.begin(), S.order_adj.end());
+      std::vector<int> dep(S.fdep_off.begin(), S.fdep_off.end());
+      dep.insert(dep.end(), S.fdep_idx.begin(), S.fdep_idx.end());
+      sb->n_pdep_f = (int)dep.size();
+      dep.insert(dep.end(), S.adep_off.begin(), S.adep_off.end());
+      dep.insert(dep.end(), S.adep_idx.begin(), S.adep_idx.end());
+      sb->n_pdep_a = (int)dep.size() - sb->n_pdep_f;
+      sb->d_porder = dalloc<int>(ord.size(), by);
+      sb->d_pdep = dalloc<int>(dep.size(), by);
+      sb->d_pdone = dalloc<int>((size_t)nt + 1, by);
+      sb->d_pctl = dalloc<int>(2, by);
+      h2d(sb->d_porder, ord, s);
+      h2d(sb->d_pdep, dep, s);
+      ck(cudaMemsetAsync(sb->d_pdone, 0, sizeof(int) * ((size_t)nt + 1), s), "memset");
+      ck(cudaMemsetAsync(sb->d_pctl, 0, sizeof(int) * 2, s), "memset");
+      int sf = 0, sa = 0;
+      for (const DTask& T : P.tasks)
+        if (T.scratch < 0) {
+          sf = std::max(sf, T.smem);
+          sa = std::max(sa, T.smem_adj);
+        }
+      sb->psmem_f = (size_t)sf * sizeof(double);
+      sb->psmem_a = (size_t)sa * sizeof(double);
+      int nbf = 0, nba = 0;
+      ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbf, k_fwd_persist<true>, kNT2L, sb->psmem_f), "occupancy");
+      ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nba, k_adj_persist, kNT2L, sb->psmem_a), "occupancy");
+      if (nbf < 1 || (adjoint && nba < 1)) throw Error(WG_ERANGE, "persistent launch does not fit on an SM");
+      sb->pgrid_f = std::min(nt, nbf * ctx->n_sm);
+      sb->pgrid_a = std::min(nt, std::max(nba, 1) * ctx->n_sm);
+    }
     {
       // priority grows (numerically falls) with the class
       const int pr = std::max(prio_hi, prio_lo - c.cls);
@@ -1731,6 +1930,8 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
   ck(cudaMallocHost(&b->h_params, sizeof(double) * (b->P + 2)), "cudaMallocHost");
   ck(cudaMallocHost(&b->h_logl, sizeof(double) * n), "cudaMallocHost");
   if (adjoint) ck(cudaMallocHost(&b->h_gred, sizeof(double) * b->P * b->subs.size()), "cudaMallocHost");
+  ck(cudaMallocHost(&b->h_perr, sizeof(int)), "cudaMallocHost");
+  *b->h_perr = 0;
   ck(cudaStreamSynchronize(s), "batch upload");
   b->ccds.assign(ccds, ccds + n);
   return b;
@@ -1886,12 +2087,35 @@ void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted, bool no
           }
         });
   };
+  // one persistent pass of a class: flags and ticket cleared, then the kernel
+  auto persist_args = [&](SubBatch* sb, bool adj) {
+    PArgs P;
+    P.order = sb->d_porder + (adj ? sb->n_tasks : 0);
+    P.dep_off = sb->d_pdep + (adj ? sb->n_pdep_f : 0);
+    P.dep_idx = P.dep_off + sb->n_tasks + 1;
+    P.done = sb->d_pdone;
+    P.ticket = sb->d_pctl;
+    P.err = sb->d_pctl + 1;
+    P.n = sb->n_tasks;
+    P.spin_cap = b->persist_spin_cap;
+    P.wait_unset = b->persist_wait_unset;
+    ck(cudaMemsetAsync(sb->d_pdone, 0, sizeof(int) * ((size_t)sb->n_tasks + 1), sb->s), "memset");
+    ck(cudaMemsetAsync(sb->d_pctl, 0, sizeof(int) * (adj ? 1 : 2), sb->s), "memset");
+    return P;
+  };
   ck(cudaEventRecordWithFlags(ctx->ev[0], s, cudaEventRecordExternal), "event");
   fork_subs(b);
   for (auto& sbp : b->subs) {
     SubBatch* sb = sbp.get();
     KArgs2 A = sub_args(b, sb);
     A.famw = weighted ? b->d_famw : nullptr;
+    if (sb->persist) {
+      const PArgs P = persist_args(sb, false);
+      ++nl;
+      if (tables) k_fwd_persist<true><<<sb->pgrid_f, kNT2L, sb->psmem_f, sb->s>>>(A, P);
+      else k_fwd_persist<false><<<sb->pgrid_f, kNT2L, sb->psmem_f, sb->s>>>(A, P);
+      continue;
+    }
     // a checkpointed class keeps no tables in the forward: its adjoint
     // recomputes them level by level
     for (int L = 0; L < (int)sb->lvl_n.size(); ++L) fwd_level(sb, A, L, tables && !sb->checkpoint);
@@ -1907,7 +2131,12 @@ void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted, bool no
       KArgs2 A = sub_args(b, sb);
       A.famw = weighted ? b->d_famw : nullptr;
       const int top = (int)sb->lvl_n.size() - 1;
-      for (int L = (int)sb->lvl_n.size() - 1; L >= 0; --L) {
+      if (sb->persist) {
+        const PArgs P = persist_args(sb, true);
+        ++nl;
+        k_adj_persist<<<sb->pgrid_a, kNT2L, sb->psmem_a, sb->s>>>(A, P);
+      }
+      for (int L = sb->persist ? -1 : (int)sb->lvl_n.size() - 1; L >= 0; --L) {
         const int* ll = sb->d_lists + sb->lvl_off[L];
         const int* lh = sb->d_lists + sb->lvlh_off[L];
         // checkpointed class: this level's tables again, from the children's
@@ -1952,6 +2181,9 @@ void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted, bool no
   }
   // results to the pinned host buffers, inside the graph: fetch only waits
   ck(cudaMemcpyAsync(b->h_logl, b->d_logl, sizeof(double) * b->NF, cudaMemcpyDeviceToHost, s), "logl download");
+  for (auto& sb : b->subs)
+    if (sb->persist)
+      ck(cudaMemcpyAsync(b->h_perr, sb->d_pctl + 1, sizeof(int), cudaMemcpyDeviceToHost, s), "error download");
   if (grad)
     for (size_t i = 0; i < b->subs.size(); ++i)
       ck(cudaMemcpyAsync(b->h_gred + i * b->P, b->subs[i]->d_gred, sizeof(double) * b->P, cudaMemcpyDeviceToHost, s),
@@ -2110,6 +2342,10 @@ void fetch(wg_batch* b, const wg_model* m, double* per_family, double* total, do
   const bool grad = b->grad_pending;
   ck(cudaStreamSynchronize(s), "evaluation");  // the graph ends with the result downloads
   b->pending = false;
+  if (b->persist && *b->h_perr) {
+    *b->h_perr = 0;
+    throw Error(WG_ECUDA, "persistent pass: a wait for a dependency ran out of polls; the results are invalid");
+  }
   b->tables_fresh = (b->flags & WG_BATCH_TABLES) != 0;
   finish_timing(b->ctx);
   std::vector<double> gred;
@@ -2186,6 +2422,9 @@ int wg_ctx_create(int device, wg_ctx** out) {
     ck(cudaFuncSetAttribute(k_fwd2<true, kNT2L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
     ck(cudaFuncSetAttribute(k_adj2<kNT2L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
     ck(cudaFuncSetAttribute(k_adj2<kNT2H>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    ck(cudaFuncSetAttribute(k_fwd_persist<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    ck(cudaFuncSetAttribute(k_fwd_persist<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    ck(cudaFuncSetAttribute(k_adj_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
     noalloc_resolve(c.get());
     *out = c.release();
   });

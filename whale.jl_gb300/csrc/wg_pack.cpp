@@ -20,6 +20,7 @@
 //     is ordered into levels of the split DAG.
 // The transposed programs the adjoint needs are built here as well.
 #include <algorithm>
+#include <limits>
 #include <array>
 #include <atomic>
 #include <cmath>
@@ -811,21 +812,30 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       const bool is_root = kind == WG_NODE_ROOT;
       const double tops_lim = is_root ? (double)opt.target_ops * opt.root_group : (double)opt.target_ops;
       const int64_t wlim = is_root ? opt.max_width_root : opt.max_width;
+      // the adjoint keeps six rows of max(width, staged children) plus the
+      // partial slots (a margin) and the branch's ϕ, ψ
+      const bool bound_smem = is_root && opt.root_smem_doubles > 0;
+      const int ka = m.ch0[k], kb = m.ch1[k];
       std::vector<int> cur;
       double ops = 0;
-      int64_t width = 0;
+      int64_t width = 0, staged = 0;
       for (auto& [w, f] : fw) {
         const int C = info[f].ncompat[k];
-        if (!cur.empty() && (ops + w > tops_lim || width + C > wlim)) {
+        const int S = (ka >= 0 ? info[f].ncompat[ka] : 0) + (kb >= 0 ? info[f].ncompat[kb] : 0);
+        const bool over_smem =
+            bound_smem && 6 * std::max(width + C, staged + S) + 2 * m.nrow[k] + 1024 > opt.root_smem_doubles;
+        if (!cur.empty() && (ops + w > tops_lim || width + C > wlim || over_smem)) {
           groups.push_back(cur);
           group_ops.push_back(ops);
           cur.clear();
           ops = 0;
           width = 0;
+          staged = 0;
         }
         cur.push_back(f);
         ops += w;
         width += C;
+        staged += S;
       }
       if (!cur.empty()) { groups.push_back(cur); group_ops.push_back(ops); }
     }
@@ -855,7 +865,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       // wide for shared memory take the wide CTAs
       const int64_t W2est = std::max<int64_t>(col[nf], (int64_t)cola[nf] + colb[nf]);
       const bool wide = (opt.adjoint ? 6 : 2) * W2est + 2 * m.nrow[k] > opt.smem_limit_doubles;
-      const int NT = (kind != WG_NODE_ROOT && (gops > opt.heavy_ops || wide)) ? kNT2H : kNT2L;
+      const int NT = (!opt.light_only && kind != WG_NODE_ROOT && (gops > opt.heavy_ops || wide)) ? kNT2H : kNT2L;
       T.nt = NT;
       const int R = col[nf];
       if (R >= 32768) throw Error(WG_ERANGE, "task row wider than 32767 clades");
@@ -1178,6 +1188,64 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
     P.red_idx.insert(P.red_idx.end(), red[j].begin(), red[j].end());
   }
   return P;
+}
+
+Schedule persistent_schedule(const Packed2& P) {
+  Schedule S;
+  const size_t H = P.levels.size();
+  for (size_t h = 0; h < H; ++h)
+    for (const auto* lv : {&P.levels[h], &P.levels_h[h], &P.levels_g[h], &P.levels_gh[h]})
+      S.order_fwd.insert(S.order_fwd.end(), lv->begin(), lv->end());
+  for (size_t h = H; h-- > 0;)
+    for (const auto* lv : {&P.levels[h], &P.levels_h[h], &P.levels_g[h], &P.levels_gh[h]})
+      S.order_adj.insert(S.order_adj.end(), lv->begin(), lv->end());
+  const int n = (int)P.tasks.size();
+  if ((int)S.order_fwd.size() != n) throw Error(WG_ESTATE, "internal: a task is in no level");
+  // the task owning each top-row offset
+  std::vector<std::pair<int64_t, int>> tops(n);
+  for (int t = 0; t < n; ++t) tops[t] = {P.tasks[t].top, t};
+  std::sort(tops.begin(), tops.end());
+  auto producer = [&](int64_t off) {
+    auto it = std::upper_bound(tops.begin(), tops.end(), std::make_pair(off, std::numeric_limits<int>::max()));
+    if (it == tops.begin()) throw Error(WG_ESTATE, "internal: staged offset before every top row");
+    const int t = std::prev(it)->second;
+    if (off >= P.tasks[t].top + P.tasks[t].width) throw Error(WG_ESTATE, "internal: staged offset in no top row");
+    return t;
+  };
+  std::vector<std::vector<int>> fdep(n), adep(n);
+  parallel_for((size_t)n, default_host_threads(), [&](size_t t) {
+    const DTask& T = P.tasks[t];
+    const int64_t ms = (int64_t)T.wa + T.wb;
+    int last = -1;
+    for (int64_t i = 0; i < ms; ++i) {
+      const int p = producer(P.gmap[T.gmap + i]);
+      if (p != last) fdep[t].push_back(p);
+      last = p;
+    }
+    std::sort(fdep[t].begin(), fdep[t].end());
+    fdep[t].erase(std::unique(fdep[t].begin(), fdep[t].end()), fdep[t].end());
+  });
+  for (int t = 0; t < n; ++t)
+    for (int p : fdep[t]) adep[p].push_back(t);
+  auto csr = [&](const std::vector<std::vector<int>>& d, std::vector<int32_t>& off, std::vector<int32_t>& idx) {
+    off.assign(n + 1, 0);
+    for (int t = 0; t < n; ++t) off[t + 1] = off[t] + (int32_t)d[t].size();
+    idx.reserve(off[n]);
+    for (int t = 0; t < n; ++t) idx.insert(idx.end(), d[t].begin(), d[t].end());
+  };
+  csr(fdep, S.fdep_off, S.fdep_idx);
+  csr(adep, S.adep_off, S.adep_idx);
+  // every wait targets an earlier ticket of its pass (no wait can block the
+  // ticket it waits for)
+  std::vector<int> pos_f(n), pos_a(n);
+  for (int i = 0; i < n; ++i) pos_f[S.order_fwd[i]] = i, pos_a[S.order_adj[i]] = i;
+  for (int t = 0; t < n; ++t) {
+    for (int p : fdep[t])
+      if (pos_f[p] >= pos_f[t]) throw Error(WG_ESTATE, "internal: forward order is not topological");
+    for (int c : adep[t])
+      if (pos_a[c] >= pos_a[t]) throw Error(WG_ESTATE, "internal: adjoint order is not topological");
+  }
+  return S;
 }
 
 // Checkpointed tables: the adjoint recomputes each height level's tables from
