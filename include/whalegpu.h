@@ -278,6 +278,27 @@ int wg_backtrack(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t family, int32_t 
 int wg_backtrack_tables(const wg_model* m, const wg_ccd* c, const double* tables, int64_t n_tables, int32_t n_samples,
                         uint64_t seed, char* out, int64_t cap, int64_t* needed);
 
+/* TreeTracker's sampling on the device (src/track.jl:180-414, :30-40): tree i
+ * of family families[i] is drawn with seed seeds[i] by one GPU thread from the
+ * DP tables of the batch's last fetched evaluation (as wg_batch_tables: the
+ * batch has WG_BATCH_TABLES), with the host sampler's event order, arithmetic
+ * and random stream, so a tree equals wg_backtrack_tables' for the same seed
+ * (n_samples = 1).  offsets[n_trees + 1] receives the prefix sums of the trees'
+ * node counts; the nodes stay in the batch until wg_track_nodes copies them.
+ * Nothing but these node arrays crosses to the host.  m: the batch's model
+ * (its structure maps clades to table columns on the first call). */
+int wg_track_device(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t n_trees, const int32_t* families,
+                    const uint64_t* seeds, int64_t* offsets);
+/* The last wg_track_device call's nodes, 4 ints each: clade (-1: loss),
+ * species node (model-order position), slice where its branch starts,
+ * parent node (-1 at the root), trees one after another, nodes in the
+ * sampler's order.  cap = nodes the buffer holds. */
+int wg_track_nodes(const wg_batch* b, int32_t* nodes, int64_t cap);
+/* One tree's node arrays (as wg_track_nodes gives them) as wg_backtrack's
+ * extended Newick line, NUL-terminated; *needed as there. */
+int wg_tree_newick(const wg_model* m, const wg_ccd* c, const int32_t* nodes, int32_t n_nodes, char* out, int64_t cap,
+                   int64_t* needed);
+
 /* Asynchronous pair for device-side timing: enqueue the evaluation on the
  * context stream (inputs already resident), then fetch the results (this
  * synchronises).  with_grad selects the adjoint. */

@@ -88,6 +88,9 @@ def _declare(L):
         "wg_logpdf_noalloc": (C.c_int, [vp, vp, vp, P_dbl, P_dbl]),
         "wg_logpdf_tables": (C.c_int, [vp, vp, vp, i32, P_dbl, i64, P_i64, P_dbl]),
         "wg_batch_tables": (C.c_int, [vp, vp, i32, P_dbl, i64, P_i64, P_dbl]),
+        "wg_track_device": (C.c_int, [vp, vp, vp, i32, P_i32, C.POINTER(C.c_uint64), P_i64]),
+        "wg_track_nodes": (C.c_int, [vp, P_i32, i64]),
+        "wg_tree_newick": (C.c_int, [vp, vp, P_i32, i32, C.c_char_p, i64, P_i64]),
         "wg_enqueue": (C.c_int, [vp, vp, vp, C.c_int]),
         "wg_fetch": (C.c_int, [vp, vp, vp, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl, P_dbl]),
         "wg_synth_family": (C.c_int, [vp, P_dbl, P_dbl, P_dbl, dbl, C.POINTER(C.c_char_p), u64, i32, i32, i32, i32,

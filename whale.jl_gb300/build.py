@@ -21,7 +21,7 @@ LIB = os.path.join(OUT, "libwhalegpu.so")
 HOST_LIB = os.path.join(OUT, "libwhalehost.so")
 
 CXX_SRCS = ["wg_api.cpp", "wg_model.cpp", "wg_ccd.cpp", "wg_pack.cpp", "wg_synth.cpp", "wg_track.cpp"]
-CU_SRCS = ["wg_kernels.cu", "wg_nowhere.cu"]
+CU_SRCS = ["wg_kernels.cu", "wg_nowhere.cu", "wg_track_dev.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -45,7 +45,7 @@ def _stale(target: str, deps) -> bool:
 
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
-    headers = [os.path.join(CSRC, "wg_internal.h"), os.path.join(CSRC, "wg_nowhere.h"),
+    headers = [os.path.join(CSRC, "wg_internal.h"), os.path.join(CSRC, "wg_nowhere.h"), os.path.join(CSRC, "wg_track_dev.h"),
                os.path.join(HERE, "..", "include", "whalegpu.h")]
     nvcc = _nvcc()
     inc = ["-I", os.path.join(_cuda_home(), "include")]

@@ -157,6 +157,18 @@ int wg_backtrack_tables(const wg_model* m, const wg_ccd* c, const double* tables
   });
 }
 
+int wg_tree_newick(const wg_model* m, const wg_ccd* c, const int32_t* nodes, int32_t n_nodes, char* out, int64_t cap,
+                   int64_t* needed) {
+  WG_GUARD({
+    if (!m || !c || !nodes) throw wg::Error(WG_EINVAL, "wg_tree_newick: bad arguments");
+    const std::string text = wg::tree_newick(*m, *c, nodes, n_nodes);
+    if (needed) *needed = (int64_t)text.size() + 1;
+    if (!out) return WG_OK;
+    if (cap < (int64_t)text.size() + 1) throw wg::Error(WG_ERANGE, "output buffer too small");
+    std::memcpy(out, text.c_str(), text.size() + 1);
+  });
+}
+
 int wg_ccd_parse_ale(const char* text, size_t len, const char* const* species_names, const int32_t* species_ids,
                      int32_t n_species, wg_ccd** out) {
   WG_GUARD({
@@ -289,13 +301,13 @@ int wg_ccd_export(const wg_ccd* c, int32_t* nleaves, int64_t* counts, int32_t* s
 }
 
 // Packing options of a batch with these flags, as wg_batch_create sets them
-// for a device with 227 KB of shared memory per CTA (one size class).
+// for a device with 228 KB of shared memory per SM (one size class).
 static wg::PackOptions2 host_pack_options(uint32_t flags) {
   wg::PackOptions2 opt;
   opt.adjoint = (flags & WG_BATCH_GRAD) != 0;
   opt.keep_tables = (flags & (WG_BATCH_GRAD | WG_BATCH_TABLES)) != 0;
   if (flags & WG_BATCH_PERSISTENT) {
-    const int64_t cap = 227 * 1024 / 8 / wg::pack_knob("WG_PERSIST_CTAS", 3, 1, 8) - 64;
+    const int64_t cap = (228 * 1024 / wg::pack_knob("WG_PERSIST_CTAS", 3, 1, 8) - 1024) / 8 - 64;
     opt.light_only = true;
     opt.root_smem_doubles = cap;
     opt.smem_limit_doubles = cap;

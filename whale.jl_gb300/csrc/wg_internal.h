@@ -386,6 +386,11 @@ std::vector<std::vector<int>> compat_columns(const Model& m, const CCD& c);
 // wg_logpdf_tables); one extended-Newick line per tree.
 std::string backtrack_family(const Model& m, const CCD& c, const double* tables, int n_samples, uint64_t seed);
 
+// One sampled tree given as node arrays (clade, species node, slice, parent;
+// nodes in the sampler's creation order) in the extended Newick of
+// backtrack_family.
+std::string tree_newick(const Model& m, const CCD& c, const int32_t* nodes, int n);
+
 }  // namespace wg
 
 // Public opaque handles are the internal types.

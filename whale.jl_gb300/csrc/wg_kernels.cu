@@ -23,6 +23,7 @@
 
 #include "wg_internal.h"
 #include "wg_nowhere.h"
+#include "wg_track_dev.h"
 
 using namespace wg;
 
@@ -1409,6 +1410,7 @@ struct wg_ctx {
   cudaEvent_t fork = nullptr, join = nullptr;
   int n_sm = 0;
   size_t smem_optin = 0;
+  size_t smem_sm = 0;  // shared memory of one SM
   bool timing = false;
   bool timed = false;  // events of the last evaluation were recorded
   bool timed_grad = false;
@@ -1526,6 +1528,43 @@ struct SubBatch {
   }
 };
 
+// Device copy of the families' structure for backtracking on the device
+// (built on the first wg_track_device call of a batch), and the buffers of
+// the last call.
+struct TrackData {
+  int device = 0;
+  int64_t* d_fk_tab = nullptr;
+  int* d_fk_w = nullptr;
+  int* d_fk_col = nullptr;
+  int64_t* d_fclade = nullptr;
+  int* d_fnclade = nullptr;
+  int64_t* d_fcol = nullptr;
+  int16_t* d_cols = nullptr;
+  int64_t* d_csplit = nullptr;
+  int* d_g1 = nullptr;
+  int* d_g2 = nullptr;
+  double* d_sp = nullptr;
+  unsigned char* d_cleaf = nullptr;
+  const double** d_ftabs = nullptr;
+  std::vector<int64_t> cap;  // per family: node slots of one tree (an upper bound)
+  // per-call buffers, grown as needed
+  int* d_fam = nullptr;
+  uint64_t* d_seed = nullptr;
+  int64_t* d_capoff = nullptr;
+  int64_t* d_off = nullptr;
+  int* d_count = nullptr;
+  int4* d_nodes = nullptr;
+  int4* d_stack = nullptr;
+  int4* d_out = nullptr;
+  size_t n_trees_cap = 0, slots_cap = 0, out_cap = 0;
+  std::vector<int32_t> last_nodes;  // the last call's trees (4 ints per node)
+  ~TrackData() {
+    free_all(device, {d_fk_tab, d_fk_w, d_fk_col, d_fclade, d_fnclade, d_fcol, d_cols, d_csplit, d_g1, d_g2, d_sp,
+                      d_cleaf, (void*)d_ftabs, d_fam, d_seed, d_capoff, d_off, d_count, d_nodes, d_stack, d_out},
+             {});
+  }
+};
+
 struct wg_batch {
   wg_ctx* ctx = nullptr;
   int K = 0, NR = 0, NF = 0, P = 0, n_tasks = 0;
@@ -1562,6 +1601,7 @@ struct wg_batch {
   // NowhereExtinctCondition on the device, forked beside the DP
   std::unique_ptr<NwPlan> nw;
   bool nw_pending = false;
+  std::unique_ptr<TrackData> track;  // device backtracking (wg_track_device)
   // captured launch sequences: [with gradient][with tables][weighted][nowhere]
   cudaGraphExec_t graph[2][2][2][2] = {};
   void drop_graphs(int nowhere) {
@@ -1577,6 +1617,7 @@ struct wg_batch {
     drop_graphs(0);
     drop_graphs(1);
     nw.reset();
+    track.reset();
     if (ctx) free_all(ctx->device, {d_famw}, {h_famw});
     plain.reset();
     subs.clear();
@@ -1729,7 +1770,10 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
   // in device memory
   b->persist = (flags & WG_BATCH_PERSISTENT) != 0;
   const int64_t pctas = pack_knob("WG_PERSIST_CTAS", 3, 1, 8);
-  const int64_t pcap = (int64_t)(ctx->smem_optin / (size_t)pctas) / (int64_t)sizeof(double) - 64;
+  // (an SM's shared memory split over pctas CTAs, less the 1 KB the
+  // hardware reserves per CTA and a margin for the kernels' static variables)
+  const int64_t pcap = std::min<int64_t>((int64_t)ctx->smem_optin, (int64_t)ctx->smem_sm / pctas - 1024) /
+                           (int64_t)sizeof(double) - 64;
   b->persist_spin_cap = (int)pack_knob("WG_PERSIST_SPIN_CAP", 1 << 22, 0, 1 << 30);
   b->persist_wait_unset = (int)pack_knob("WG_PERSIST_TEST_UNSET_WAIT", 0, 0, 1);
   const int single_class[] = {1 << 30};
@@ -2407,6 +2451,8 @@ int wg_ctx_create(int device, wg_ctx** out) {
     int v = 0;
     ck(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device), "attr");
     c->n_sm = v;
+    ck(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device), "attr");
+    c->smem_sm = (size_t)v;
     ck(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "attr");
     c->smem_optin = (size_t)v;
     ck(cudaFuncSetAttribute(k_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
@@ -2422,9 +2468,18 @@ int wg_ctx_create(int device, wg_ctx** out) {
     ck(cudaFuncSetAttribute(k_fwd2<true, kNT2L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
     ck(cudaFuncSetAttribute(k_adj2<kNT2L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
     ck(cudaFuncSetAttribute(k_adj2<kNT2H>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_fwd_persist<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_fwd_persist<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_adj_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
+    // the persistent kernels hold a little static shared memory (the ticket)
+    auto dyn_max = [&](const void* fn) {
+      cudaFuncAttributes fa;
+      ck(cudaFuncGetAttributes(&fa, fn), "attr");
+      return v - (int)fa.sharedSizeBytes;
+    };
+    ck(cudaFuncSetAttribute(k_fwd_persist<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            dyn_max((const void*)k_fwd_persist<true>)), "attr");
+    ck(cudaFuncSetAttribute(k_fwd_persist<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            dyn_max((const void*)k_fwd_persist<false>)), "attr");
+    ck(cudaFuncSetAttribute(k_adj_persist, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            dyn_max((const void*)k_adj_persist)), "attr");
     noalloc_resolve(c.get());
     *out = c.release();
   });
@@ -2675,6 +2730,196 @@ int wg_batch_tables(wg_ctx* ctx, wg_batch* b, int32_t family, double* out, int64
       o += (int64_t)b->nrow[k] * nc;
     }
     ck(cudaStreamSynchronize(s), "table download");
+  });
+}
+
+}  // extern "C"
+
+namespace {
+
+// Species-tree height in nodes (root to deepest leaf, WGD nodes counted).
+int tree_height(const wg_model* m) {
+  std::vector<int> h(m->K, 0);
+  for (int k = 0; k < m->K; ++k)  // children precede parents in the order
+    for (int c : {m->ch0[k], m->ch1[k]})
+      if (c >= 0) h[k] = std::max(h[k], h[c] + 1);
+  return h[m->K - 1];
+}
+
+template <class T>
+T* upload_vec(const std::vector<T>& v, cudaStream_t s) {
+  int64_t by = 0;
+  T* d = dalloc<T>(v.size(), by);
+  h2d(d, v, s);
+  return d;
+}
+
+std::unique_ptr<TrackData> build_track(wg_batch* b, const wg_model* m) {
+  const int K = b->K, NF = b->NF;
+  cudaStream_t s = b->ctx->stream;
+  auto td = std::make_unique<TrackData>();
+  td->device = b->ctx->device;
+  std::vector<int64_t> fk_tab((size_t)NF * K), fclade(NF), fcol(NF), csplit;
+  std::vector<int> fk_w((size_t)NF * K), fk_col((size_t)NF * K), fnclade(NF), g1, g2;
+  std::vector<int16_t> cols;
+  std::vector<double> sp;
+  std::vector<unsigned char> cleaf;
+  std::vector<const double*> ftabs(NF);
+  const int H = tree_height(m);
+  td->cap.resize(NF);
+  int64_t nsplit = 0;
+  for (int f = 0; f < NF; ++f) {
+    const SubBatch* sb = b->subs[b->fam_sub[f]].get();
+    const size_t lf = (size_t)b->fam_local[f];
+    const CCD& c = *b->ccds[f];
+    ftabs[f] = sb->d_tabs;
+    for (int k = 0; k < K; ++k) {
+      const size_t fk = (size_t)f * K + k, lk = lf * K + k;
+      fk_tab[fk] = sb->fam_tab[lk];
+      fk_w[fk] = sb->fam_w[lk];
+      fk_col[fk] = sb->fam_col[lk];
+    }
+    fclade[f] = (int64_t)cleaf.size();
+    fnclade[f] = c.n_clades;
+    fcol[f] = (int64_t)cols.size();
+    const auto cc = compat_columns(*m, c);
+    for (int k = 0; k < K; ++k)
+      for (int g = 0; g < c.n_clades; ++g) cols.push_back((int16_t)cc[k][g]);
+    for (int g = 0; g < c.n_clades; ++g) {
+      csplit.push_back(nsplit + c.split_off[g]);
+      cleaf.push_back(c.nleaves[g] == 1 ? 1 : 0);
+    }
+    nsplit += c.split_off[c.n_clades];
+    g1.insert(g1.end(), c.g1.begin(), c.g1.end());
+    g2.insert(g2.end(), c.g2.begin(), c.g2.end());
+    sp.insert(sp.end(), c.p.begin(), c.p.end());
+    // every gene-tree edge crosses at most H + 1 species nodes, each crossing
+    // at most one node and one loss
+    td->cap[f] = 2 * (2 * (int64_t)std::max(c.n_genes, 1)) * (H + 1) + 8;
+  }
+  csplit.push_back(nsplit);
+  td->d_fk_tab = upload_vec(fk_tab, s);
+  td->d_fk_w = upload_vec(fk_w, s);
+  td->d_fk_col = upload_vec(fk_col, s);
+  td->d_fclade = upload_vec(fclade, s);
+  td->d_fnclade = upload_vec(fnclade, s);
+  td->d_fcol = upload_vec(fcol, s);
+  td->d_cols = upload_vec(cols, s);
+  td->d_csplit = upload_vec(csplit, s);
+  td->d_g1 = upload_vec(g1, s);
+  td->d_g2 = upload_vec(g2, s);
+  td->d_sp = upload_vec(sp, s);
+  td->d_cleaf = upload_vec(cleaf, s);
+  td->d_ftabs = upload_vec(ftabs, s);
+  ck(cudaStreamSynchronize(s), "track upload");
+  return td;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wg_track_device(wg_ctx* ctx, wg_model* m, wg_batch* b, int32_t n_trees, const int32_t* families,
+                    const uint64_t* seeds, int64_t* offsets) {
+  WG_GUARD({
+    if (!ctx || !m || !b || b->ctx != ctx || n_trees < 0 || (n_trees > 0 && (!families || !seeds)) || !offsets)
+      throw Error(WG_EINVAL, "wg_track_device: bad arguments");
+    if (!(b->flags & WG_BATCH_TABLES)) throw Error(WG_ESTATE, "batch was created without WG_BATCH_TABLES");
+    if (m->K != b->K || m->total_rows() != b->NR) throw Error(WG_EINVAL, "batch was built for a different model");
+    if (b->pending || !b->tables_fresh)
+      throw Error(WG_ESTATE, "no fetched evaluation of this batch holds its tables (evaluate it first)");
+    for (int i = 0; i < n_trees; ++i)
+      if (families[i] < 0 || families[i] >= b->NF) throw Error(WG_EINVAL, "family index out of range");
+    ck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t s = ctx->stream;
+    if (!b->track) b->track = build_track(b, m);
+    TrackData& td = *b->track;
+    const size_t n = (size_t)n_trees;
+    std::vector<int64_t> cap_off(n + 1, 0);
+    for (size_t i = 0; i < n; ++i) cap_off[i + 1] = cap_off[i] + td.cap[families[i]];
+    int64_t by = 0;
+    if (n + 1 > td.n_trees_cap) {
+      free_all(td.device, {td.d_fam, td.d_seed, td.d_count, td.d_capoff, td.d_off}, {});
+      td.d_fam = nullptr, td.d_seed = nullptr, td.d_count = nullptr, td.d_capoff = nullptr, td.d_off = nullptr;
+      td.d_fam = dalloc<int>(n + 1, by);
+      td.d_seed = dalloc<uint64_t>(n + 1, by);
+      td.d_count = dalloc<int>(n + 1, by);
+      td.d_capoff = dalloc<int64_t>(n + 1, by);
+      td.d_off = dalloc<int64_t>(n + 1, by);
+      td.n_trees_cap = n + 1;
+    }
+    const size_t slots = (size_t)std::max<int64_t>(cap_off[n], 1);
+    if (slots > td.slots_cap) {
+      free_all(td.device, {td.d_nodes, td.d_stack}, {});
+      td.d_nodes = nullptr, td.d_stack = nullptr;
+      td.d_nodes = dalloc<int4>(slots, by);
+      td.d_stack = dalloc<int4>(slots, by);
+      td.slots_cap = slots;
+    }
+    ck(cudaMemcpyAsync(td.d_fam, families, sizeof(int) * n, cudaMemcpyHostToDevice, s), "upload");
+    ck(cudaMemcpyAsync(td.d_seed, seeds, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, s), "upload");
+    ck(cudaMemcpyAsync(td.d_capoff, cap_off.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s), "upload");
+    TrackArgs A;
+    A.K = b->K;
+    A.NR = b->NR;
+    A.mnode = b->d_mnode;
+    A.row_off = b->d_rowoff;
+    A.params = b->d_params;
+    A.ftabs = td.d_ftabs;
+    A.fk_tab = td.d_fk_tab;
+    A.fk_w = td.d_fk_w;
+    A.fk_col = td.d_fk_col;
+    A.fclade = td.d_fclade;
+    A.fnclade = td.d_fnclade;
+    A.fcol = td.d_fcol;
+    A.cols = td.d_cols;
+    A.csplit = td.d_csplit;
+    A.g1 = td.d_g1;
+    A.g2 = td.d_g2;
+    A.sp = td.d_sp;
+    A.cleaf = td.d_cleaf;
+    A.n = n_trees;
+    A.fam = td.d_fam;
+    A.seed = td.d_seed;
+    A.cap_off = td.d_capoff;
+    A.nodes = td.d_nodes;
+    A.stack = td.d_stack;
+    A.count = td.d_count;
+    ck(track_launch(A, s), "track launch");
+    std::vector<int> count(n);
+    ck(cudaMemcpyAsync(count.data(), td.d_count, sizeof(int) * n, cudaMemcpyDeviceToHost, s), "download");
+    ck(cudaStreamSynchronize(s), "track");
+    offsets[0] = 0;
+    for (size_t i = 0; i < n; ++i) {
+      if (count[i] == kTrackOverflow) throw Error(WG_ERANGE, "a sampled tree exceeds its node capacity");
+      if (count[i] == kTrackNoEvent) throw Error(WG_ESTATE, "backtracking found no event with positive probability");
+      if (count[i] == kTrackNoLikelihood) throw Error(WG_ESTATE, "backtracking needs a family with positive likelihood");
+      offsets[i + 1] = offsets[i] + count[i];
+    }
+    const size_t total = (size_t)offsets[n];
+    if (std::max<size_t>(total, 1) > td.out_cap) {
+      free_all(td.device, {td.d_out}, {});
+      td.d_out = nullptr;
+      td.d_out = dalloc<int4>(std::max<size_t>(total, 1), by);
+      td.out_cap = std::max<size_t>(total, 1);
+    }
+    ck(cudaMemcpyAsync(td.d_off, offsets, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s), "upload");
+    ck(track_compact(td.d_nodes, td.d_capoff, td.d_off, td.d_out, n_trees, s), "track compaction");
+    td.last_nodes.resize(4 * total);
+    if (total)
+      ck(cudaMemcpyAsync(td.last_nodes.data(), td.d_out, sizeof(int4) * total, cudaMemcpyDeviceToHost, s),
+         "download");
+    ck(cudaStreamSynchronize(s), "track");
+  });
+}
+
+int wg_track_nodes(const wg_batch* b, int32_t* nodes, int64_t cap) {
+  WG_GUARD({
+    if (!b || !nodes) throw Error(WG_EINVAL, "wg_track_nodes: bad arguments");
+    if (!b->track) throw Error(WG_ESTATE, "no wg_track_device call on this batch");
+    const auto& v = b->track->last_nodes;
+    if (cap < (int64_t)(v.size() / 4)) throw Error(WG_ERANGE, "output buffer too small");
+    if (!v.empty()) std::memcpy(nodes, v.data(), v.size() * sizeof(int32_t));
   });
 }
 

@@ -288,6 +288,21 @@ std::string to_newick(const Model& m, const CCD& c, const std::vector<RecNode>& 
 
 }  // namespace
 
+std::string tree_newick(const Model& m, const CCD& c, const int32_t* nodes, int n) {
+  if (n < 1) throw Error(WG_EINVAL, "a tree has at least its root");
+  std::vector<RecNode> t((size_t)n);
+  for (int i = 0; i < n; ++i) {
+    const int32_t* x = nodes + 4 * (size_t)i;
+    if (x[1] < 0 || x[1] >= m.K || x[0] < -1 || x[0] >= c.n_clades || x[3] >= i || (x[3] < 0) != (i == 0))
+      throw Error(WG_EINVAL, "malformed tree node arrays");
+    t[i] = {x[0], x[1], x[2], x[3], {}};
+    if (x[3] >= 0) t[x[3]].ch.push_back(i);
+  }
+  // a node's children were made in one step, in reverse of the sampler's order
+  for (auto& r : t) std::reverse(r.ch.begin(), r.ch.end());
+  return to_newick(m, c, t);
+}
+
 std::string backtrack_family(const Model& m, const CCD& c, const double* tables, int n_samples, uint64_t seed) {
   const std::vector<std::vector<int>> cols = compat_columns(m, c);
   Tracker tr(m, c, tables, cols);

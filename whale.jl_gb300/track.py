@@ -248,8 +248,42 @@ def track_tables(tables_of, wm: WhaleModel, ccds: Sequence[CCD], draws: Sequence
     return [sumtrees(t, c, wm) for t, c in zip(trees, ccds)]
 
 
+def sample_device(b, wm: WhaleModel, families: Sequence[int], seeds: Sequence[int]):
+    """One reconciled tree per (family, seed) sampled on the device from the
+    tables of the batch's last fetched evaluation (wg_track_device); each
+    equals ``backtrack_tables(..., n=1, seed)`` on the same tables.  Returns
+    the node arrays (per tree an (n, 4) int32 array: clade, species node,
+    slice, parent)."""
+    import numpy as np
+
+    fam = np.ascontiguousarray(families, dtype=np.int32)
+    sd = np.ascontiguousarray(seeds, dtype=np.uint64)
+    off = np.zeros(fam.size + 1, dtype=np.int64)
+    L = N.lib()
+    N.check(L.wg_track_device(b.ctx.h, wm._struct.h, b.h, int(fam.size), N.iptr(fam),
+                              sd.ctypes.data_as(C.POINTER(C.c_uint64)), N.lptr(off)))
+    nodes = np.zeros((max(int(off[-1]), 1), 4), dtype=np.int32)
+    N.check(L.wg_track_nodes(b.h, nodes.ctypes.data_as(N.P_i32), nodes.shape[0]))
+    return [nodes[off[i]:off[i + 1]] for i in range(fam.size)]
+
+
+def tree_of_nodes(wm: WhaleModel, ccd: CCD, nodes) -> RecTree:
+    """A sampled tree's node arrays as a RecTree (wg_tree_newick)."""
+    import numpy as np
+
+    a = np.ascontiguousarray(nodes, dtype=np.int32)
+    L = N.lib()
+    need = N.i64()
+    N.check(L.wg_tree_newick(wm._struct.h, ccd._h, a.ctypes.data_as(N.P_i32), a.shape[0], None, 0, C.byref(need)))
+    buf = C.create_string_buffer(need.value)
+    N.check(L.wg_tree_newick(wm._struct.h, ccd._h, a.ctypes.data_as(N.P_i32), a.shape[0], buf, need.value,
+                             C.byref(need)))
+    text = buf.value.decode()
+    return RecTree(text, _parse(text, wm))
+
+
 def track(wm: WhaleModel, ccds: Sequence[CCD], draws: Sequence, n: int, fun=None, seed: int = 0,
-          summary: bool = True, threads: int = 0):
+          summary: bool = True, threads: int = 0, device: bool = True):
     """``track(TreeTracker(wm, ccds, draws, fun), n)`` (src/track.jl:11-82):
     ``n`` reconciled trees per family from the posterior predictive, each
     under a draw picked uniformly from ``draws`` (``fun(wm, draw)`` gives the
@@ -262,9 +296,32 @@ def track(wm: WhaleModel, ccds: Sequence[CCD], draws: Sequence, n: int, fun=None
     tree per family from its tables on ``threads`` host threads (0: every
     core).  All families of a pick share
     its draw (the reference picks per family): each family's trees have the
-    same distribution.  The same seed gives the same trees."""
+    same distribution.  The same seed gives the same trees.
+
+    With ``device`` (the default) every pick's trees are sampled on the GPU,
+    one thread per family, from the tables in device memory
+    (wg_track_device); only the sampled node arrays come back.  Otherwise
+    each family's tables are downloaded and sampled on host threads.  Both
+    give the same trees."""
     wm.load()
     b = get_batch(wm, list(ccds), tables=True)
+    if device:
+        import numpy as np
+
+        if len(draws) == 0:
+            raise ValueError("no posterior draws")
+        picks = np.random.default_rng(seed).integers(len(draws), size=int(n))
+        trees = [[] for _ in ccds]
+        fams = list(range(len(ccds)))
+        for j, i in enumerate(picks):
+            m = fun(wm, draws[i]) if fun is not None else wm(draws[i])
+            b.logpdf(m)
+            arrs = sample_device(b, m, fams, [_draw_seed(seed, j, f) for f in fams])
+            for f, a in enumerate(arrs):
+                trees[f].append(tree_of_nodes(m, ccds[f], a))
+        if not summary:
+            return trees
+        return [sumtrees(t, c, wm) for t, c in zip(trees, ccds)]
     state = {"model": None}
 
     def tables_of(m, f):
