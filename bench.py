@@ -231,6 +231,78 @@ def pick_cpu_sample(W, wl, budget_s, threads):
     return list(order[:k])
 
 
+def run_track(args, W):
+    """TreeTracker sampling of one pick, 1 tree per family of the workload,
+    timed both ways after one batched logpdf! (tables in device memory):
+    device (wg_track_device + wg_track_nodes: one thread per tree, node
+    arrays back) and host (wg_batch_tables download per family +
+    wg_backtrack_tables on every host core).  Both give the same trees."""
+    import ctypes as C
+    from concurrent.futures import ThreadPoolExecutor
+
+    import torch
+    from whale_gb300 import synth
+    from whale_gb300 import _native as N
+    from whale_gb300.track import _draw_seed, sample_device
+
+    wl = make_workload(synth, args.config, args.families, 0)
+    wm, ccds = wl.model, wl.ccds()
+    b = W.Batch(wm, ccds, tables=True)
+    b.logpdf(wm)
+    nf = len(ccds)
+    fams = list(range(nf))
+    seeds = [_draw_seed(0, 0, f) for f in fams]
+    L = N.lib()
+    wm.load()
+    dev = []
+    for _ in range(3 + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        arrs = sample_device(b, wm, fams, seeds)
+        dev.append(time.perf_counter() - t0)
+    dev = dev[3:]
+    nodes = sum(a.shape[0] for a in arrs)
+
+    def host_one(f):
+        need = N.i64()
+        N.check(L.wg_batch_tables(b.ctx.h, b.h, f, None, 0, C.byref(need), None))
+        tab = np.zeros(max(need.value, 1))
+        N.check(L.wg_batch_tables(b.ctx.h, b.h, f, N.dptr(tab), need.value, C.byref(need), None))
+        N.check(L.wg_backtrack_tables(wm._struct.h, ccds[f]._h, N.dptr(tab), tab.size, 1, C.c_uint64(seeds[f]), None,
+                                      0, C.byref(need)))
+        buf = C.create_string_buffer(need.value)
+        N.check(L.wg_backtrack_tables(wm._struct.h, ccds[f]._h, N.dptr(tab), tab.size, 1, C.c_uint64(seeds[f]), buf,
+                                      need.value, C.byref(need)))
+        return len(buf.value)
+
+    threads = os.cpu_count() or 1
+    host = []
+    with ThreadPoolExecutor(max_workers=threads) as pool:
+        for _ in range(1 + max(1, args.steps // 10)):
+            t0 = time.perf_counter()
+            list(pool.map(host_one, fams))
+            host.append(time.perf_counter() - t0)
+    host = host[1:]
+    # W.track end to end (one pick, trees parsed into RecTrees), both ways
+    wt = {}
+    for dv in (True, False):
+        t0 = time.perf_counter()
+        W.track(wm, ccds, [wm.rates], 1, seed=0, summary=False, device=dv)
+        wt[dv] = time.perf_counter() - t0
+    line = {"metric": "reconciled trees sampled per second (1 tree per family per pick, TreeTracker)",
+            "value": nf / float(np.median(dev)), "unit": "trees/s", "n_gpus": 1, "steps": args.steps,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload(nf, args.config), "families": nf, "nodes_per_pick": int(nodes)},
+            "device": {"ms_per_pick": 1e3 * float(np.median(dev)),
+                       "what": "wg_track_device + wg_track_nodes (one GPU thread per tree, node arrays to the host)"},
+            "host": {"ms_per_pick": 1e3 * float(np.median(host)), "threads": threads,
+                     "what": "per family: wg_batch_tables download + wg_backtrack_tables (host sampler and text)"},
+            "speedup": float(np.median(host)) / float(np.median(dev)),
+            "W.track_one_pick_s": {"device": wt[True], "host": wt[False],
+                                   "what": "batched logpdf! + sampling + text + RecTree parsing per family"}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, W, rank):
     if rank != 0:
         return
@@ -278,6 +350,8 @@ def main():
     ap.add_argument("--config", type=int, default=1, choices=[1, 4],
                     help="1: 5,000 families on 17 taxa (default); 4: 50,000 families on 40 taxa")
     ap.add_argument("--families", type=int, default=None, help="default: 5,000 (config 1), 50,000 (config 4)")
+    ap.add_argument("--track", action="store_true",
+                    help="time TreeTracker sampling (device vs host) instead of the likelihood")
     ap.add_argument("--persistent", action="store_true",
                     help="one persistent launch per pass instead of one launch per height level and size class")
     ap.add_argument("--checkpoint", action="store_true",
@@ -302,6 +376,9 @@ def main():
     W = __graft_entry__.load_package()
     if args.impl == "reference":
         run_reference(args, W, rank)
+        return
+    if args.track:
+        run_track(args, W)
         return
     import torch
 

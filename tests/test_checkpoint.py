@@ -33,7 +33,8 @@ def test_checkpoint_layout_holds_one_level(W):
     full, tasks = _pack(W, wm, ccds, N.BATCH_GRAD)
     kept, tasks_c = _pack(W, wm, ccds, N.BATCH_GRAD | N.BATCH_CHECKPOINT)
     assert np.array_equal(tasks, tasks_c)  # the same tasks and programs
-    per_task = nrow[tasks[:, 0]].astype(np.int64) * tasks[:, 2]
+    stride = tasks[:, 2] + (tasks[:, 2] & 1)  # table rows of an even number of doubles
+    per_task = nrow[tasks[:, 0]].astype(np.int64) * stride
     assert full == per_task.sum()
     levels = tasks[:, 1]
     by_level = [per_task[levels == h].sum() for h in np.unique(levels)]

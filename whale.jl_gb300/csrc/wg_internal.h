@@ -304,7 +304,7 @@ struct DTask {
   int64_t scratch = -1;  // rows wider than shared memory: offset of the task's working rows in the
                          // batch's device scratch (doubles); -1: the rows live in shared memory
   int32_t smem_adj = 0;  // shared doubles needed (adjoint)
-  int32_t _pad2 = 0;
+  int32_t tstride = 0;   // doubles between the DP-table rows: width rounded up to even (rows start 16-byte aligned)
 };
 
 struct Packed2 {

@@ -240,6 +240,7 @@ struct KArgs2 {
   double* logl;
   double* scratch;  // working rows of the tasks too wide for shared memory
   const double* famw;  // adjoint seed weight per family (null: 1)
+  int* err;            // error bits of the evaluation (bit 1: a bulk-copy wait ran out)
   int NR, K;
 };
 
@@ -258,16 +259,47 @@ __device__ __forceinline__ Raw decode(const ulonglong2 r) {
   return x;
 }
 
-// Asynchronous global -> shared copies (LDGSTS), 8 bytes per thread and
-// element, tracked in per-thread commit groups.
-__device__ __forceinline__ void cp_async8(double* dst, const double* src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+// 1-D bulk copies (the TMA engine) from this GPU's memory into the CTA's own
+// shared memory, each completing on an mbarrier with its byte count.  Both
+// addresses are 16-byte aligned and the size a multiple of 16.
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* mb) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mb)) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+__device__ __forceinline__ void mbar_inval(uint64_t* mb) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(mb)) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// shared memory the generic proxy touched, ordered before the bulk copies' writes
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_row_g2s(void* dst, const void* src, unsigned bytes, uint64_t* mb) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mb)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(mb))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* mb, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(mb)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for a phase of an mbarrier; false (and the error bit 2 set)
+// when the poll limit ran out.
+constexpr int kMbarPolls = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t* mb, unsigned parity, int* err) {
+  for (int i = 0; i < kMbarPolls; ++i)
+    if (mbar_try_wait(mb, parity)) return true;
+  if (err) atomicOr(err, 2);
+  return false;
 }
 
 // L1 prefetch of a lane's entries of a program (and of the thread's first
@@ -625,7 +657,7 @@ __device__ __forceinline__ void fwd_task(const KArgs2& A, const DTask& T, int ro
   const int k = T.node;
   const int4 mn = A.mnode[k];
   const int R = T.width;
-  const int W2 = max(R, T.wa + T.wb);
+  const int W2 = (max(R, T.wa + T.wb) + 1) & ~1;  // even: 16-byte aligned row buffers
   const int tid = threadIdx.x;
   const int lane = (tid + 32 * (int)(rot & (NT / 32 - 1))) & (NT - 1);
   double* cur = sm;
@@ -702,8 +734,9 @@ __device__ __forceinline__ void fwd_task(const KArgs2& A, const DTask& T, int ro
     }
     __syncthreads();
     double* tab0 = TABLES ? A.tabs + T.tab : nullptr;
-    if (!fwd_rows_dispatch<NT, TABLES>(T.dup.J, E, T, lane, mn.w, R, phs, pss, cur, nxt, part, tab0))
-      fwd_rows_generic<NT, TABLES>(E, T, lane, mn.w, R, phs, pss, cur, nxt, part, tab0);
+    // (the row loops use the width only as the tables' row stride)
+    if (!fwd_rows_dispatch<NT, TABLES>(T.dup.J, E, T, lane, mn.w, T.tstride, phs, pss, cur, nxt, part, tab0))
+      fwd_rows_generic<NT, TABLES>(E, T, lane, mn.w, T.tstride, phs, pss, cur, nxt, part, tab0);
   }
   double* top = A.tops + T.top;
   for (int c = tid; c < R; c += NT) top[c] = cur[c];
@@ -725,7 +758,7 @@ __device__ __forceinline__ void fwd_task(const KArgs2& A, const DTask& T, int ro
 // memory; the code is otherwise the same.
 template <bool TABLES, int NT, bool ROOT = false, bool GLOBAL = false>
 __global__ void __launch_bounds__(NT) k_fwd2(const KArgs2 A, const int* __restrict__ list) {
-  extern __shared__ double smem_dyn[];
+  extern __shared__ __align__(128) double smem_dyn[];
   fwd_task<TABLES, NT, ROOT, GLOBAL, false>(A, A.tasks[list[blockIdx.x]], (int)blockIdx.x, smem_dyn);
 }
 
@@ -840,13 +873,16 @@ __device__ __forceinline__ void block_sum4(double (&v)[4], double* red) {
 // forms the row adjoints after the sum over tasks.  Branches with a row whose
 // ψ is below kPsiOneDot (or ϕ = 0) take both dots directly (ONEDOT false,
 // entries streamed) and write ∂/∂ϕ_r, ∂/∂ψ_r to out[2r], out[2r + 1].
-// GMEM: the task's rows live in device memory (plain copies, no cp.async).
+// GMEM: the task's rows live in device memory (plain copies, no bulk copies).
+// Otherwise each table row goes to its shared buffer as one 1-D bulk copy
+// (TMA) issued by thread 0 and completed on that buffer's mbarrier (mb[3]).
 template <int NT, int J, bool ONEDOT, bool GMEM>
 __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTask& T, int lane, int n, int R,
                                          const double* phs, const double* pss, double*& bar, double*& barn,
                                          double* Lb, int W2, double* Gs, double* part, double* red,
-                                         const double* tab0, double* out) {
+                                         const double* tab0, double* out, uint64_t* mb, int* err) {
   const int tid = threadIdx.x, wid = tid >> 5, wl = tid & 31;
+  const int S = T.tstride;  // table row stride (even: rows 16-byte aligned)
   double rp[8], rs[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) rp[i] = rs[i] = 0.0;
@@ -854,22 +890,38 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
   LaneProg<(J > 0 ? J : 1)> lp;
   if (J > 0) load_lane_prog<(J > 0 ? J : 1)>(E, td, lane, lp);
   const bool active = lane < td.nt;
-  // Row r reads table row r-1 from buffer (n-1-r) mod 3 (buffer i at Lb +
-  // i·W2); the copies run two rows ahead, one commit group per row (empty
-  // past row 1).
-  auto fetch = [&](int rr, double* dst) {
-    if (rr >= 1) {
-      const double* src = tab0 + (int64_t)(rr - 1) * R;
-      if constexpr (GMEM)
-        for (int c = tid; c < R; c += NT) dst[c] = src[c];
-      else
-        for (int c = tid; c < R; c += NT) cp_async8(dst + c, src + c);
+  if constexpr (!GMEM) {
+    // the buffers may hold what generic stores left (an earlier task's rows)
+    fence_proxy_async_smem();
+    if (tid == 0) {
+      for (int i = 0; i < 3; ++i) mbar_init(mb + i);
+      mbar_init_fence();
     }
-    cp_async_commit();
+    __syncthreads();
+  }
+  // Row r reads table row r-1 from buffer (n-1-r) mod 3 (buffer i at Lb +
+  // i·W2); the copies run two rows ahead (none past row 1).  par: bit i is
+  // the phase parity of buffer i's next completion.
+  unsigned par = 0;
+  auto fetch = [&](int rr, int buf) {
+    if (rr < 1) return;
+    const double* src = tab0 + (int64_t)(rr - 1) * S;
+    double* dst = Lb + buf * W2;
+    if constexpr (GMEM) {
+      for (int c = tid; c < R; c += NT) dst[c] = src[c];
+    } else if (tid == 0) {
+      bulk_row_g2s(dst, src, (unsigned)S * 8u, mb + buf);
+    }
+  };
+  auto landed = [&](int buf) {  // buffer buf's copy has arrived (every thread waits)
+    if constexpr (!GMEM) {
+      mbar_wait(mb + buf, (par >> buf) & 1u, err);
+      par ^= 1u << buf;
+    }
   };
   constexpr int NW = NT / 32;
   if constexpr (ONEDOT) {  // E_{n-1} = Σ bar_{n-1}·L_{n-1}
-    const double* Ltop = tab0 + (int64_t)(n - 1) * R;
+    const double* Ltop = tab0 + (int64_t)(n - 1) * S;
     double e = 0.0;
     for (int c = tid; c < R; c += NT) e = fma(bar[c], Ltop[c], e);
     for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
@@ -921,23 +973,23 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
     }
   };
   int bi = 0;
-  fetch(n - 1, Lb);
-  fetch(n - 2, Lb + W2);
+  fetch(n - 1, 0);
+  fetch(n - 2, 1);
   if constexpr (ONEDOT) {
     // One CTA barrier per row: it follows the program (bar_{r-1} complete)
-    // once each thread's copies of the next row's table row have landed.
-    // The dot reads only bar_{r-1} and row r-1, which the next program does
-    // not write, and a buffer is refilled only after the barrier that
-    // follows its last reader (the dot of the row above).
-    cp_async_wait<1>();
+    // once the next row's table row has landed.  The dot reads only
+    // bar_{r-1} and row r-1, which the next program does not write, and a
+    // buffer is refilled only after the barrier that follows its last reader
+    // (the dot of the row above).
+    landed(0);
     __syncthreads();
     for (int r = n - 1; r >= 1; --r) {
       double* Lp = Lb + bi * W2;
       double* bn = barn;
       row(r, Lp, bar, bn);
-      cp_async_wait<0>();
+      if (r >= 2) landed(bi == 2 ? 0 : bi + 1);
       __syncthreads();
-      fetch(r - 2, Lb + (bi == 0 ? 2 : bi - 1) * W2);  // row r+1's buffer takes table row r-3
+      fetch(r - 2, bi == 0 ? 2 : bi - 1);  // row r+1's buffer takes table row r-3
       bi = bi == 2 ? 0 : bi + 1;
       const int slot = (n - 1 - r) & 7;
       double e = 0.0;  // this lane's share of E_{r-1}
@@ -964,10 +1016,10 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
   } else {
     for (int r = n - 1; r >= 1; --r) {
       double* Lp = Lb + bi * W2;
-      cp_async_wait<1>();
+      landed(bi);
       __syncthreads();
       // every thread is past row r+1, whose buffer takes table row r-3
-      fetch(r - 2, Lb + (bi == 0 ? 2 : bi - 1) * W2);
+      fetch(r - 2, bi == 0 ? 2 : bi - 1);
       bi = bi == 2 ? 0 : bi + 1;
       const double* bb = bar;
       row(r, Lp, bb, barn);
@@ -1004,24 +1056,30 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
       barn = t;
     }
   }
-  cp_async_wait<0>();  // only empty groups remain; row 0 reuses the buffers
+  if constexpr (!GMEM) {  // every copy was waited for; row 0 reuses the buffers
+    __syncthreads();
+    if (tid == 0)
+      for (int i = 0; i < 3; ++i) mbar_inval(mb + i);
+  }
 }
 
 template <int NT, bool GMEM, int J = kAdjJStep>
 __device__ __forceinline__ bool adj_rows_dispatch(int j, const DEntry* __restrict__ E, const DTask& T, int lane, int n,
                                                   int R, const double* phs, const double* pss, double*& bar,
                                                   double*& barn, double* Lb, int W2, double* Gs, double* part,
-                                                  double* red, const double* tab0, double* out) {
+                                                  double* red, const double* tab0, double* out, uint64_t* mb,
+                                                  int* err) {
   constexpr int MAXJ = NT == kNT2L ? 8 : 12;
   if constexpr (J > MAXJ) {
     return false;
   } else {
     constexpr int NEXT = (J + kAdjJStep > MAXJ && J < MAXJ) ? MAXJ : J + kAdjJStep;
     if (j <= J) {
-      adj_rows<NT, J, true, GMEM>(E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out);
+      adj_rows<NT, J, true, GMEM>(E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out, mb, err);
       return true;
     }
-    return adj_rows_dispatch<NT, GMEM, NEXT>(j, E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out);
+    return adj_rows_dispatch<NT, GMEM, NEXT>(j, E, T, lane, n, R, phs, pss, bar, barn, Lb, W2, Gs, part, red, tab0, out,
+                                             mb, err);
   }
 }
 
@@ -1033,7 +1091,7 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
   const int k = T.node;
   const int4 mn = A.mnode[k];
   const int R = T.width;
-  const int W2 = max(R, T.wa + T.wb);
+  const int W2 = (max(R, T.wa + T.wb) + 1) & ~1;  // even: 16-byte aligned row buffers
   const int tid = threadIdx.x;
   const int lane = (tid + 32 * (int)(rot & (NT / 32 - 1))) & (NT - 1);
   const int NR = A.NR;
@@ -1165,11 +1223,14 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
     // one-dot row adjoints unless a row's ψ is tiny (uniform over the CTA)
     bool ok = true;
     for (int r = 1 + tid; r < n; r += NT) ok &= pss[r] >= kPsiOneDot && phs[r] > 0.0;
+    __shared__ __align__(8) uint64_t mb[3];  // the table-row buffers' mbarriers
     if (!__syncthreads_and(ok))
-      adj_rows<NT, 0, false, GLOBAL>(E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red, tab0, out);
+      adj_rows<NT, 0, false, GLOBAL>(E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red, tab0, out, mb,
+                                     A.err);
     else if (!adj_rows_dispatch<NT, GLOBAL>(T.tdup.J, E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red,
-                                           tab0, out))
-      adj_rows<NT, 0, true, GLOBAL>(E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red, tab0, out);
+                                           tab0, out, mb, A.err))
+      adj_rows<NT, 0, true, GLOBAL>(E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red, tab0, out, mb,
+                                    A.err);
   }
   __syncthreads();
   // ---- row 0
@@ -1249,7 +1310,7 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
 template <int NT, bool ROOT = false, bool GLOBAL = false>
 __global__ void __launch_bounds__(NT, NT == 128 && !GLOBAL ? 4 : (GLOBAL ? 1 : 2))
     k_adj2(const KArgs2 A, const int* __restrict__ list) {
-  extern __shared__ double smem_dyn[];
+  extern __shared__ __align__(128) double smem_dyn[];
   adj_task<NT, ROOT, GLOBAL, false>(A, A.tasks[list[blockIdx.x]], (int)blockIdx.x, smem_dyn);
 }
 
@@ -1334,7 +1395,7 @@ __device__ __forceinline__ void publish(const PArgs& P, int task) {
 // largest of the layout's shared-memory tasks.
 template <bool TABLES>
 __global__ void __launch_bounds__(kNT2L, 4) k_fwd_persist(const KArgs2 A, const PArgs P) {
-  extern __shared__ double smem_dyn[];
+  extern __shared__ __align__(128) double smem_dyn[];
   __shared__ int s_t;
   for (;;) {
     if (threadIdx.x == 0) s_t = atomicAdd(P.ticket, 1);
@@ -1356,7 +1417,7 @@ __global__ void __launch_bounds__(kNT2L, 4) k_fwd_persist(const KArgs2 A, const 
 
 // Persistent adjoint, tickets from the root level down.
 __global__ void __launch_bounds__(kNT2L, 4) k_adj_persist(const KArgs2 A, const PArgs P) {
-  extern __shared__ double smem_dyn[];
+  extern __shared__ __align__(128) double smem_dyn[];
   __shared__ int s_t;
   for (;;) {
     if (threadIdx.x == 0) s_t = atomicAdd(P.ticket, 1);
@@ -1573,7 +1634,8 @@ struct wg_batch {
   double flops_fwd = 0, bytes_fwd = 0, flops_adj = 0;
   int64_t tab_full = 0, tab_kept = 0;  // table doubles: every table / held on the device
   bool persist = false;                // persistent launches (WG_BATCH_PERSISTENT)
-  int* h_perr = nullptr;               // error bits of the last evaluation's persistent passes (pinned)
+  int* d_err = nullptr;                // error bits of an evaluation: 1 dependency wait, 2 bulk-copy wait
+  int* h_perr = nullptr;               // the last evaluation's error bits (pinned)
   int persist_spin_cap = 1 << 22, persist_wait_unset = 0;
   int n_checkpointed = 0;              // size classes that recompute their tables per level
   std::vector<std::unique_ptr<SubBatch>> subs;
@@ -1621,7 +1683,8 @@ struct wg_batch {
     if (ctx) free_all(ctx->device, {d_famw}, {h_famw});
     plain.reset();
     subs.clear();
-    if (ctx) free_all(ctx->device, {d_mnode, d_rowoff, d_leafp, d_params, d_logl}, {h_params, h_logl, h_gred, h_perr});
+    if (ctx)
+      free_all(ctx->device, {d_mnode, d_rowoff, d_leafp, d_params, d_logl, d_err}, {h_params, h_logl, h_gred, h_perr});
   }
 };
 
@@ -1793,7 +1856,8 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
     opt.adjoint = adjoint;
     opt.keep_tables = keep;
     opt.global_ids = &ids;
-    opt.smem_limit_doubles = (flags & WG_BATCH_SCRATCH_ROWS) ? 0 : (int64_t)(ctx->smem_optin / sizeof(double));
+    // (a little below the opt-in size: the kernels' static shared variables)
+    opt.smem_limit_doubles = (flags & WG_BATCH_SCRATCH_ROWS) ? 0 : (int64_t)(ctx->smem_optin / sizeof(double)) - 32;
     if (b->persist) {
       opt.light_only = true;
       opt.root_smem_doubles = pcap;
@@ -1970,6 +2034,8 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
   }
   b->d_params = dalloc<double>(b->P + 2, by);
   b->d_logl = dalloc<double>(n, by);
+  b->d_err = dalloc<int>(1, by);
+  ck(cudaMemsetAsync(b->d_err, 0, sizeof(int), s), "memset");
   upload_model_static(b.get(), m, s);
   ck(cudaMallocHost(&b->h_params, sizeof(double) * (b->P + 2)), "cudaMallocHost");
   ck(cudaMallocHost(&b->h_logl, sizeof(double) * n), "cudaMallocHost");
@@ -1999,6 +2065,7 @@ KArgs2 sub_args(const wg_batch* b, const SubBatch* sb) {
   A.logl = b->d_logl;
   A.scratch = sb->d_scratch;
   A.famw = nullptr;
+  A.err = b->d_err;
   A.NR = b->NR;
   A.K = b->K;
   return A;
@@ -2075,6 +2142,7 @@ void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted, bool no
   nl = 0;
   ck(cudaMemcpyAsync(b->d_params, b->h_params, sizeof(double) * (b->P + 2), cudaMemcpyHostToDevice, s),
      "params upload");
+  ck(cudaMemsetAsync(b->d_err, 0, sizeof(int), s), "memset");
   if (nowhere) {  // the condition depends on the rates only: beside the DP
     NwPlan& p = *b->nw;
     ck(cudaEventRecord(p.fork, s), "event");
@@ -2139,12 +2207,12 @@ void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted, bool no
     P.dep_idx = P.dep_off + sb->n_tasks + 1;
     P.done = sb->d_pdone;
     P.ticket = sb->d_pctl;
-    P.err = sb->d_pctl + 1;
+    P.err = b->d_err;
     P.n = sb->n_tasks;
     P.spin_cap = b->persist_spin_cap;
     P.wait_unset = b->persist_wait_unset;
     ck(cudaMemsetAsync(sb->d_pdone, 0, sizeof(int) * ((size_t)sb->n_tasks + 1), sb->s), "memset");
-    ck(cudaMemsetAsync(sb->d_pctl, 0, sizeof(int) * (adj ? 1 : 2), sb->s), "memset");
+    ck(cudaMemsetAsync(sb->d_pctl, 0, sizeof(int), sb->s), "memset");
     return P;
   };
   ck(cudaEventRecordWithFlags(ctx->ev[0], s, cudaEventRecordExternal), "event");
@@ -2225,9 +2293,7 @@ void record_sequence(wg_batch* b, bool grad, bool tables, bool weighted, bool no
   }
   // results to the pinned host buffers, inside the graph: fetch only waits
   ck(cudaMemcpyAsync(b->h_logl, b->d_logl, sizeof(double) * b->NF, cudaMemcpyDeviceToHost, s), "logl download");
-  for (auto& sb : b->subs)
-    if (sb->persist)
-      ck(cudaMemcpyAsync(b->h_perr, sb->d_pctl + 1, sizeof(int), cudaMemcpyDeviceToHost, s), "error download");
+  ck(cudaMemcpyAsync(b->h_perr, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, s), "error download");
   if (grad)
     for (size_t i = 0; i < b->subs.size(); ++i)
       ck(cudaMemcpyAsync(b->h_gred + i * b->P, b->subs[i]->d_gred, sizeof(double) * b->P, cudaMemcpyDeviceToHost, s),
@@ -2386,9 +2452,11 @@ void fetch(wg_batch* b, const wg_model* m, double* per_family, double* total, do
   const bool grad = b->grad_pending;
   ck(cudaStreamSynchronize(s), "evaluation");  // the graph ends with the result downloads
   b->pending = false;
-  if (b->persist && *b->h_perr) {
+  if (const int e = *b->h_perr) {
     *b->h_perr = 0;
-    throw Error(WG_ECUDA, "persistent pass: a wait for a dependency ran out of polls; the results are invalid");
+    throw Error(WG_ECUDA, std::string(e & 1 ? "persistent pass: a wait for a dependency ran out of polls"
+                                            : "adjoint: a wait for a bulk copy ran out of polls") +
+                              "; the results are invalid");
   }
   b->tables_fresh = (b->flags & WG_BATCH_TABLES) != 0;
   finish_timing(b->ctx);
@@ -2459,27 +2527,25 @@ int wg_ctx_create(int device, wg_ctx** out) {
     ck(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking), "cudaStreamCreate");
     ck(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming), "cudaEventCreate");
     ck(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming), "cudaEventCreate");
-    ck(cudaFuncSetAttribute(k_fwd2<false, kNT2L>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_fwd2<true, kNT2L>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_fwd2<false, kNT2H>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_fwd2<true, kNT2H>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_adj2<kNT2L>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_fwd2<false, kNT2L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_fwd2<true, kNT2L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_adj2<kNT2L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    ck(cudaFuncSetAttribute(k_adj2<kNT2H>, cudaFuncAttributeMaxDynamicSharedMemorySize, v), "attr");
-    // the persistent kernels hold a little static shared memory (the ticket)
-    auto dyn_max = [&](const void* fn) {
+    // the largest dynamic shared memory every kernel may request: the
+    // opt-in size less its own static shared variables
+    auto set_dyn_max = [&](const void* fn) {
       cudaFuncAttributes fa;
       ck(cudaFuncGetAttributes(&fa, fn), "attr");
-      return v - (int)fa.sharedSizeBytes;
+      ck(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, v - (int)fa.sharedSizeBytes), "attr");
     };
-    ck(cudaFuncSetAttribute(k_fwd_persist<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            dyn_max((const void*)k_fwd_persist<true>)), "attr");
-    ck(cudaFuncSetAttribute(k_fwd_persist<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            dyn_max((const void*)k_fwd_persist<false>)), "attr");
-    ck(cudaFuncSetAttribute(k_adj_persist, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            dyn_max((const void*)k_adj_persist)), "attr");
+    set_dyn_max((const void*)k_fwd2<false, kNT2L>);
+    set_dyn_max((const void*)k_fwd2<true, kNT2L>);
+    set_dyn_max((const void*)k_fwd2<false, kNT2H>);
+    set_dyn_max((const void*)k_fwd2<true, kNT2H>);
+    set_dyn_max((const void*)k_fwd2<false, kNT2L, true>);
+    set_dyn_max((const void*)k_fwd2<true, kNT2L, true>);
+    set_dyn_max((const void*)k_adj2<kNT2L>);
+    set_dyn_max((const void*)k_adj2<kNT2L, true>);
+    set_dyn_max((const void*)k_adj2<kNT2H>);
+    set_dyn_max((const void*)k_fwd_persist<true>);
+    set_dyn_max((const void*)k_fwd_persist<false>);
+    set_dyn_max((const void*)k_adj_persist);
     noalloc_resolve(c.get());
     *out = c.release();
   });

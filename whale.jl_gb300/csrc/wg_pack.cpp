@@ -1037,7 +1037,9 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       slots = std::max(slots, T.rslot);  // root: the level programs' partial slots
       // forward: cur, nxt (children staged in nxt); adjoint: bar, barn, two
       // L rows, G; then partial slots and reduction scratch
-      const int W2 = std::max(R, T.wa + T.wb);
+      // row buffers of an even number of doubles (16-byte aligned rows)
+      const int W2r = std::max(R, T.wa + T.wb);
+      const int W2 = W2r + (W2r & 1);
       T.nslot_max = slots;
       // + the branch's ϕ and ψ rows staged in shared memory
       T.smem = 2 * W2 + slots + 2 * m.nrow[k] + 16 * (NT / 32) + 32;
@@ -1077,15 +1079,18 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
       const int R = T.width, NT = tb.NT, smem_adj = tb.smem_adj;
       T.top = P.tops_doubles;
       P.tops_doubles += R;
+      // table rows of an even number of doubles: every row starts on a
+      // 16-byte boundary (bulk copies into shared memory)
+      T.tstride = R + (R & 1);
       if (opt.keep_tables) {
         T.tab = P.tab_doubles;
-        P.tab_doubles += (int64_t)m.nrow[k] * R;
+        P.tab_doubles += (int64_t)m.nrow[k] * T.tstride;
       }
       for (int i = 0; i < nf; ++i) {
         const size_t fk = (size_t)fams[i] * K + k;
         toploc[fk] = T.top + tb.col[i];
         P.fam_tab[fk] = T.tab;
-        P.fam_w[fk] = R;
+        P.fam_w[fk] = T.tstride;
         P.fam_col[fk] = tb.col[i];
         P.fam_ncol[fk] = info[fams[i]].ncompat[k];
       }
@@ -1262,7 +1267,7 @@ int64_t checkpoint_tables(Packed2& P, const Model& m) {
       for (int t : *lv) {
         DTask& T = P.tasks[t];
         T.tab = off;
-        off += (int64_t)m.nrow[T.node] * T.width;
+        off += (int64_t)m.nrow[T.node] * T.tstride;
       }
     need = std::max(need, off);
   }
