@@ -303,6 +303,25 @@ def run_track(args, W):
     print(json.dumps(line), flush=True)
 
 
+def run_tune(args, W):
+    """The autotuner on the workload: coordinate descent over the packing
+    knobs, the size-class bounds, each class's CTA shape and the launch
+    layout, timed by CUDA events; prints the chosen shape per class and its
+    time against the defaults."""
+    from whale_gb300 import autotune, synth
+
+    wl = make_workload(synth, args.config, args.families, 0)
+    wm, ccds = wl.model, wl.ccds()
+    nb = {"classes": tuple(range(len(autotune.CLASS_BOUNDS))), "persistent": (0, 1),
+          **{f"heavy_c{i}": (0, 512, 2048, 1 << 20) for i in range(autotune.N_CLASSES)},
+          "target_ops": (320, 480, 720), "target_j": (2, 3, 4), "root_group": (8, 16, 32)}
+    best, b, log = W.tune(wm, ccds, steps=max(3, args.steps), warmup=3, neighbours=nb, rounds=2)
+    rep = autotune.report(best, log)
+    rep.update({"metric": "autotuned ms per gradient evaluation", "config": {"workload": workload(len(ccds),
+                args.config), "families": len(ccds)}, "unit": "ms", "higher_is_better": False})
+    print(json.dumps(rep), flush=True)
+
+
 def run_reference(args, W, rank):
     if rank != 0:
         return
@@ -350,6 +369,7 @@ def main():
     ap.add_argument("--config", type=int, default=1, choices=[1, 4],
                     help="1: 5,000 families on 17 taxa (default); 4: 50,000 families on 40 taxa")
     ap.add_argument("--families", type=int, default=None, help="default: 5,000 (config 1), 50,000 (config 4)")
+    ap.add_argument("--tune", action="store_true", help="run the autotuner on the workload and report its choice")
     ap.add_argument("--track", action="store_true",
                     help="time TreeTracker sampling (device vs host) instead of the likelihood")
     ap.add_argument("--persistent", action="store_true",
@@ -379,6 +399,9 @@ def main():
         return
     if args.track:
         run_track(args, W)
+        return
+    if args.tune:
+        run_tune(args, W)
         return
     import torch
 
@@ -485,8 +508,7 @@ def main():
     K = len(wm.order)
     h2d = 8 * (3 * NR + K + 3)  # slice tables, q, η and the two root-row constants
     # per-family log L plus one gradient vector per size class of the batch
-    # (clade-count classes bounded at 128, 256, 512, 1024, 1536)
-    n_cls = len({int(np.searchsorted([128, 256, 512, 1024, 1536], c.n_clades, side="left")) for c in ccds})
+    n_cls = batch.tables_layout()[0]
     d2h = 8 * NF + 8 * (3 * NR + K + 1) * n_cls
     # forward alone (for the gradient-cost ratio) and the plain one-family-per-launch path
     fwd_only = []

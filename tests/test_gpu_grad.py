@@ -148,3 +148,23 @@ def test_gradient_tiny_duplication_rate_two_dot_rows(W, O):
     # λ ~ 1e-5: ψ below the one-dot threshold on every branch, the two-dot form
     g, og = _slow_rates_case(W, O, 1e-5, 0.01)
     assert _close(g, og) <= GREL
+
+
+@pytest.mark.parametrize("log_lam", [-5.0, -7.0, -9.0])
+def test_one_dot_row_adjoints_with_small_duplication_term(W, O, ex1_tree, ex1_files, log_lam):
+    # low duplication and high loss on every branch: ψ per slice is 2.5e-4 down
+    # to 4.6e-6 (above the 1e-6 switch to the two-dot form), so the ψ term is a
+    # tiny share of each row's dot and ∂ψ_r = (E_{r-1} - E_r)/ψ_r is a
+    # difference of nearly equal sums; the gradient must still match the duals
+    t = W.readnw(ex1_tree)
+    lam = np.full(17, log_lam)
+    mu = np.full(17, np.log(3.0))
+    wm = W.WhaleModel(W.DLWGD(λ=lam, μ=mu, q=[0.3, 0.45], η=0.7), t, 0.05)
+    ccds = W.read_ale(os.path.dirname(ex1_files[0]), wm)
+    tot, gd = W.logpdf_gradient(wm, ccds)
+    g = np.concatenate([gd["λ"], gd["μ"], gd["q"], [gd["η"]]])
+    om = O.OracleModel(ex1_tree, 0.05)
+    otot, og = om.gradient(O.read_ale_files(om, ex1_files), lam, mu, q=[0.3, 0.45], eta=0.7)
+    assert np.isfinite(otot)
+    assert tot == pytest.approx(otot, rel=1e-10)
+    assert _close(g, og) <= GREL

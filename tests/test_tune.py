@@ -59,6 +59,27 @@ def test_descent_finds_the_optimum_of_a_known_cost(W):
     def cost(s):
         return 1.0 + sum(abs(np.log(s[k] / target[k])) for k in target)
 
-    best, batch, log = tune.tune(None, [], measure=cost)
-    assert best == target and batch is None
-    assert log[0][0] == tune.DEFAULTS and min(ms for _, ms in log) == cost(target)
+    nb = {k: tune.NEIGHBOURS[k] for k in target}
+    best, batch, log = tune.tune(None, [], measure=cost, neighbours=nb)
+    assert {k: best[k] for k in target} == target and batch is None
+    assert all(log[0][0][k] == tune.DEFAULTS[k] for k in target) and min(ms for _, ms in log) == cost(target)
+
+
+def test_shape_knobs_reach_the_environment(W):
+    # the size-class bounds, the per-class CTA shapes and the layout are
+    # knobs too: class bounds and per-class 256-thread thresholds go to the
+    # packer's environment, a class threshold of 0 follows heavy_ops
+    import os
+
+    from whale_gb300 import autotune as tune
+
+    with tune.packing({"classes": 1, "heavy_c2": 2048, "heavy_c3": 0, "persist_ctas": 4}):
+        assert os.environ["WG_CLASS_BOUNDS"] == ",".join(map(str, tune.CLASS_BOUNDS[1]))
+        assert os.environ["WG_PACK_HEAVY_OPS_C2"] == "2048"
+        assert "WG_PACK_HEAVY_OPS_C3" not in os.environ
+        assert os.environ["WG_PERSIST_CTAS"] == "4"
+    assert "WG_CLASS_BOUNDS" not in os.environ and "WG_PACK_HEAVY_OPS_C2" not in os.environ
+    sh = tune.shapes({"classes": 1, "heavy_ops": 1024, "heavy_c0": 256})
+    assert [x["clades"] for x in sh] == [(1, 128), (129, 512), (513, 1536), (1537, None)]
+    assert sh[0]["heavy_ops"] == 256 and sh[1]["heavy_ops"] == 1024
+    assert tune.shapes({"persistent": 1, "persist_ctas": 4})[0]["ctas_per_sm"] == 4

@@ -9,6 +9,13 @@ The packer's knobs decide how a batch maps onto the GPU:
               levels together): how many families share a root task
   heavy_ops   operations per row above which a non-root task gets 256
               threads instead of 128
+  heavy_c<i>  the same threshold for size class i alone (0 = heavy_ops):
+              the CTA shape of each size bucket
+  classes     which clade-count bounds split the families into size
+              classes (an index into CLASS_BOUNDS; each class is packed and
+              launched on its own, its launches sized for its tasks)
+  persistent  1: one persistent launch per pass instead of the level
+              launches (WG_BATCH_PERSISTENT), with persist_ctas CTAs per SM
 
 ``tune(wm, ccds)`` builds the batch under candidate settings, times a few
 evaluations of each on the device (CUDA events around the launch sequence,
@@ -34,15 +41,58 @@ import numpy as np
 
 from . import _native as N
 
-DEFAULTS: Dict[str, int] = {"target_ops": 480, "target_j": 3, "root_group": 16, "heavy_ops": 1024}
+# size-class bounds (clade counts) the ``classes`` knob chooses from; the
+# first is the library's default
+CLASS_BOUNDS: Tuple[Tuple[int, ...], ...] = (
+    (128, 256, 512, 1024, 1536),
+    (128, 512, 1536),
+    (64, 128, 256, 512, 1024, 1536),
+    (256, 1024),
+    (),
+)
+N_CLASSES = max(len(b) for b in CLASS_BOUNDS) + 1
+
+DEFAULTS: Dict[str, int] = {"target_ops": 480, "target_j": 3, "root_group": 16, "heavy_ops": 1024,
+                            **{f"heavy_c{i}": 0 for i in range(N_CLASSES)},
+                            "classes": 0, "persistent": 0, "persist_ctas": 3}
 NEIGHBOURS: Dict[str, Tuple[int, ...]] = {
     "target_ops": (240, 320, 480, 720, 960),
     "target_j": (2, 3, 4, 5),
     "root_group": (4, 8, 16, 32),
     "heavy_ops": (512, 1024, 2048),
+    **{f"heavy_c{i}": (0, 256, 512, 2048, 1 << 20) for i in range(N_CLASSES)},
+    "classes": tuple(range(len(CLASS_BOUNDS))),
+    "persistent": (0, 1),
 }
 _ENV = {"target_ops": "WG_PACK_TARGET_OPS", "target_j": "WG_PACK_TARGET_J", "root_group": "WG_PACK_ROOT_GROUP",
-        "heavy_ops": "WG_PACK_HEAVY_OPS"}
+        "heavy_ops": "WG_PACK_HEAVY_OPS", **{f"heavy_c{i}": f"WG_PACK_HEAVY_OPS_C{i}" for i in range(N_CLASSES)},
+        "classes": "WG_CLASS_BOUNDS", "persistent": None, "persist_ctas": "WG_PERSIST_CTAS"}
+
+
+def _env_value(knob: str, v: int):
+    """The environment string of a knob's value (None: unset)."""
+    if knob == "classes":
+        b = CLASS_BOUNDS[int(v)]
+        return ",".join(str(x) for x in b) if b else "1073741823"
+    if knob.startswith("heavy_c") and int(v) == 0:
+        return None  # the class follows heavy_ops
+    return str(int(v))
+
+
+def shapes(setting: Dict[str, int]) -> List[Dict[str, object]]:
+    """Per size class of a setting: its clade-count range and the operations
+    per row above which its non-root tasks take 256-thread CTAs (root tasks
+    always take 128), or the persistent launch's single class."""
+    if setting.get("persistent"):
+        return [{"clades": (1, None), "threads": 128, "layout": "persistent",
+                 "ctas_per_sm": setting.get("persist_ctas", 3)}]
+    b = CLASS_BOUNDS[setting.get("classes", 0)]
+    out, lo = [], 1
+    for i, hi in enumerate(list(b) + [None]):
+        h = setting.get(f"heavy_c{i}", 0) or setting.get("heavy_ops", 1024)
+        out.append({"clades": (lo, hi), "threads": (128, 256), "heavy_ops": h, "layout": "levels"})
+        lo = (hi or 0) + 1
+    return out
 _env_lock = threading.RLock()  # nested settings restore in order
 
 
@@ -52,15 +102,24 @@ def packing(setting: Dict[str, int]):
     process-wide environment variables: a batch another thread creates
     meanwhile packs with them too."""
     with _env_lock:
-        old = {k: os.environ.get(v) for k, v in _ENV.items()}
+        old = {k: os.environ.get(v) for k, v in _ENV.items() if v is not None}
+        old.update({k: None for k, v in _ENV.items() if v is None})
         try:
             for k, v in setting.items():
                 if k not in _ENV:
                     raise KeyError(f"unknown packing knob {k!r}")
-                os.environ[_ENV[k]] = str(int(v))
+                if _ENV[k] is None:
+                    continue  # a batch flag, not an environment knob
+                e = _env_value(k, v)
+                if e is None:
+                    os.environ.pop(_ENV[k], None)
+                else:
+                    os.environ[_ENV[k]] = e
             yield
         finally:
             for k, v in old.items():
+                if _ENV[k] is None:
+                    continue
                 if v is None:
                     os.environ.pop(_ENV[k], None)
                 else:
@@ -104,8 +163,9 @@ def tune(wm, ccds: Sequence, grad: bool = True, steps: int = 5, warmup: int = 2,
     from .core import Batch, default_context
 
     neighbours = dict(NEIGHBOURS if neighbours is None else neighbours)
+    start = {k: v for k, v in DEFAULTS.items() if k in neighbours or k in ("heavy_ops", "persist_ctas")}
     if measure is not None:
-        best, _, log = _descend(measure, DEFAULTS, neighbours, min_gain, rounds)
+        best, _, log = _descend(measure, start, neighbours, min_gain, rounds)
         return best, None, log
     ctx = ctx or default_context()
     L = N.lib()
@@ -115,7 +175,7 @@ def tune(wm, ccds: Sequence, grad: bool = True, steps: int = 5, warmup: int = 2,
 
     def device_ms(setting):
         with packing(setting):
-            b = Batch(wm, ccds, grad=grad, ctx=ctx)
+            b = Batch(wm, ccds, grad=grad, ctx=ctx, persistent=bool(setting.get("persistent", 0)))
         times = []
         for i in range(warmup + steps):
             if grad:
@@ -133,9 +193,20 @@ def tune(wm, ccds: Sequence, grad: bool = True, steps: int = 5, warmup: int = 2,
             kept.update(key=tuple(sorted(setting.items())), ms=ms, batch=b)
         return ms
 
-    best, _, log = _descend(device_ms, DEFAULTS, neighbours, min_gain, rounds)
+    best, _, log = _descend(device_ms, start, neighbours, min_gain, rounds)
     if kept["key"] != tuple(sorted(best.items())):
         kept["batch"] = None
         with packing(best):
-            kept["batch"] = Batch(wm, ccds, grad=grad, ctx=ctx)
+            kept["batch"] = Batch(wm, ccds, grad=grad, ctx=ctx, persistent=bool(best.get("persistent", 0)))
     return best, kept["batch"], log
+
+
+def report(best: Dict[str, int], log: List) -> Dict[str, object]:
+    """The tuned setting against the library's defaults: per size class its
+    clade range and CTA shape (``shapes``), the milliseconds per evaluation
+    of the defaults (the first setting timed) and of the best setting."""
+    default_ms = log[0][1]
+    best_ms = min(ms for s, ms in log if all(s.get(k) == v for k, v in best.items()))
+    return {"setting": dict(best), "shapes": shapes(best), "default_shapes": shapes(log[0][0]),
+            "default_ms": default_ms, "best_ms": best_ms, "speedup": default_ms / best_ms,
+            "candidates": len(log)}

@@ -1773,6 +1773,28 @@ KArgs plain_args(const PlainBatch* b) {
 // higher stream priorities, so their CTAs are dispatched first.
 constexpr int kClassBounds[] = {128, 256, 512, 1024, 1536, 1 << 30};
 
+// The size classes' upper bounds: WG_CLASS_BOUNDS (increasing clade counts,
+// comma-separated, at most 7; a last class takes the rest), else the above.
+std::vector<int> class_bounds() {
+  const char* e = std::getenv("WG_CLASS_BOUNDS");
+  if (!e || !*e) return std::vector<int>(std::begin(kClassBounds), std::end(kClassBounds));
+  std::vector<int> v;
+  const char* p = e;
+  while (*p) {
+    char* end = nullptr;
+    const long x = std::strtol(p, &end, 10);
+    if (end == p || x < 1 || x >= (1 << 30) || (!v.empty() && x <= v.back()))
+      throw Error(WG_EINVAL, "WG_CLASS_BOUNDS is not an increasing list of clade counts");
+    v.push_back((int)x);
+    p = end;
+    if (*p == ',') ++p;
+    else if (*p) throw Error(WG_EINVAL, "WG_CLASS_BOUNDS is not an increasing list of clade counts");
+  }
+  if (v.size() > 7) throw Error(WG_EINVAL, "WG_CLASS_BOUNDS: at most 7 bounds");
+  v.push_back(1 << 30);
+  return v;
+}
+
 // Device bytes of a packed class other than its tables.
 int64_t class_other_bytes(const Packed2& P, bool adjoint, int P_params) {
   int64_t by = (int64_t)(P.tasks.size() * sizeof(DTask) + P.entries.size() * sizeof(DEntry) +
@@ -1839,11 +1861,8 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
                            (int64_t)sizeof(double) - 64;
   b->persist_spin_cap = (int)pack_knob("WG_PERSIST_SPIN_CAP", 1 << 22, 0, 1 << 30);
   b->persist_wait_unset = (int)pack_knob("WG_PERSIST_TEST_UNSET_WAIT", 0, 0, 1);
-  const int single_class[] = {1 << 30};
-  const int* bounds_begin = b->persist ? single_class : kClassBounds;
-  const int* bounds_end = b->persist ? single_class + 1 : kClassBounds + sizeof(kClassBounds) / sizeof(int);
-  for (const int* bp = bounds_begin; bp != bounds_end; ++bp) {
-    const int bound = *bp;
+  std::vector<int> bounds = b->persist ? std::vector<int>{1 << 30} : class_bounds();
+  for (const int bound : bounds) {
     ++cls;
     std::vector<int> ids;
     for (int i = 0; i < n; ++i)
@@ -1858,6 +1877,8 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
     opt.global_ids = &ids;
     // (a little below the opt-in size: the kernels' static shared variables)
     opt.smem_limit_doubles = (flags & WG_BATCH_SCRATCH_ROWS) ? 0 : (int64_t)(ctx->smem_optin / sizeof(double)) - 32;
+    // per-class threshold of the 256-thread tasks (WG_PACK_HEAVY_OPS_C<class>)
+    opt.heavy_ops = pack_knob(("WG_PACK_HEAVY_OPS_C" + std::to_string(cls)).c_str(), opt.heavy_ops, 32, 1 << 20);
     if (b->persist) {
       opt.light_only = true;
       opt.root_smem_doubles = pcap;
