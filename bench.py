@@ -531,24 +531,49 @@ def main():
         plain = {"forward_ms": plain_ms, "fd_evaluations": 2 * P + 1,
                  "value": NF / ((2 * P + 1) * plain_ms * 1e-3), "unit": UNIT,
                  "what": "plain path (one family per launch) differentiated by central differences"}
-    # roofline of the dominant kernel (the adjoint or the forward)
-    fa = float(np.mean(a_ms)), float(np.mean(f_ms))
+    # The timed launch sequence overlaps each size class's adjoint with the
+    # other classes' forwards, so its roofline is that of every launch of the
+    # evaluation (k_fwd2 + k_adj2 + k_reduce2): their algorithmic FLOPs over
+    # the evaluation's CUDA-event time.  The kernels' own rooflines come from
+    # the same steps on a batch built with WG_ADJ_OVERLAP=0 (forward, then
+    # adjoint, each timed on its own).
     prof = ncu_traffic() if NF == 5000 else None
-    if fa[0] >= fa[1]:
-        kname, kms, kflops = "k_adj2 (all levels and size classes)", fa[0], batch.flops_adj
-        traffic = prof["adjoint"] if prof else None
-    else:
-        kname, kms, kflops = "k_fwd2<true> (all levels and size classes)", fa[1], batch.flops_fwd
-        traffic = prof["forward"] if prof else None
-    achieved = kflops / (kms * 1e-3) / 1e12
-    roof = {"bound": "fp64", "kernel": kname, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-            "frac": achieved / fp64_peak if fp64_peak else None, "traffic": traffic,
-            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum over the kernel's launches of one "
-                              "evaluation, one ncu capture of this workload (profiles/launches_cfg1_5000fam.txt"
-                              + (f", commit {prof['commit']}" if prof and prof.get("commit") else "") + ")",
-            "peak_source": "measured in this run: register-resident DFMA loop (wg_probe_fp64); "
-                           "MEASURED_PEAKS.json has no FP64 figure",
-            "algorithmic_flops_per_launch": kflops, "launch_ms": kms}
+    kflops = batch.flops_fwd + batch.flops_adj
+    achieved = kflops / (dev_step * 1e-3) / 1e12
+    peak_source = ("measured in this run: register-resident DFMA loop (wg_probe_fp64); "
+                   "MEASURED_PEAKS.json has no FP64 figure")
+    traffic_source = ("dram__bytes_read.sum + dram__bytes_write.sum over the kernels' launches of one evaluation, "
+                      "one ncu capture of this workload (profiles/launches_cfg1_5000fam.txt"
+                      + (f", commit {prof['commit']}" if prof and prof.get("commit") else "") + ")")
+    roof = {"bound": "fp64", "kernel": "k_fwd2 + k_adj2 (every launch of the gradient evaluation, all levels and "
+                                       "size classes)",
+            "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": achieved / fp64_peak if fp64_peak else None,
+            "traffic": (prof["adjoint"] + prof["forward"]) if prof else None, "traffic_source": traffic_source,
+            "peak_source": peak_source, "algorithmic_flops_per_launch": kflops, "launch_ms": dev_step}
+    os.environ["WG_ADJ_OVERLAP"] = "0"
+    try:
+        sep = W.Batch(wm, ccds, grad=True, ctx=ctx, checkpoint=args.checkpoint, persistent=args.persistent)
+    finally:
+        os.environ.pop("WG_ADJ_OVERLAP", None)
+    for m in models[: args.warmup]:
+        step(m, sep.h)
+    sf, sa = [], []
+    for m in models[: min(len(models), 300)]:
+        _, f, a, r = step(m, sep.h)
+        sf.append(f)
+        sa.append(a)
+    del sep
+    fa = float(np.mean(sa)), float(np.mean(sf))
+    adj_achieved = batch.flops_adj / (fa[0] * 1e-3) / 1e12
+    kernels_alone = {
+        "what": "the same steps with each size class's adjoint after every class's forward (WG_ADJ_OVERLAP=0)",
+        "ms_per_step": fa[0] + fa[1], "forward_ms": fa[1], "adjoint_ms": fa[0],
+        "adjoint_roofline": {"bound": "fp64", "kernel": "k_adj2 (all levels and size classes)",
+                             "achieved": adj_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                             "frac": adj_achieved / fp64_peak if fp64_peak else None,
+                             "traffic": prof["adjoint"] if prof else None, "traffic_source": traffic_source,
+                             "algorithmic_flops_per_launch": batch.flops_adj, "launch_ms": fa[0]}}
     # the forward's own HBM figure: its algorithmic bytes over its own time
     fwd_hbm = {"kernel": "k_fwd2<true> (all levels and size classes)", "algorithmic_bytes": batch.bytes_fwd,
                "ms": fa[1], "gbs": batch.bytes_fwd / (fa[1] * 1e-3) / 1e9,
@@ -575,6 +600,7 @@ def main():
                       "reduce": float(np.mean(r_ms)), "forward_only": fwd_only_ms},
         "grad_cost_vs_forward": dev_step / fwd_only_ms,
         "roofline": roof,
+        "kernels_alone": kernels_alone,
         "forward_hbm": fwd_hbm,
         "plain_fd": plain,
         "speedup_vs_plain_fd": (value / plain["value"]) if plain else None,

@@ -90,7 +90,11 @@ int wg_ctx_create(int device, wg_ctx** out);
 int wg_ctx_destroy(wg_ctx* ctx);
 void* wg_ctx_stream(wg_ctx* ctx); /* the cudaStream_t all work is issued on */
 /* Per-kernel device timing (CUDA events on the context stream) of the last
- * evaluation: forward, adjoint and group-reduction kernels, milliseconds. */
+ * evaluation: forward, adjoint and group-reduction kernels, milliseconds.
+ * A size class's adjoint starts when its own forward is done (unless
+ * WG_ADJ_OVERLAP=0 when the batch is created), so in a gradient evaluation
+ * the split between the first two is where the last class's forward ended;
+ * their sum is the evaluation's device time. */
 int wg_ctx_set_timing(wg_ctx* ctx, int enable);
 int wg_ctx_timings(wg_ctx* ctx, float* forward_ms, float* adjoint_ms, float* reduce_ms);
 /* Measured FP64 FMA throughput of this device (TFLOP/s), from a short

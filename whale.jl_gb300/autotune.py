@@ -16,6 +16,9 @@ The packer's knobs decide how a batch maps onto the GPU:
               launched on its own, its launches sized for its tasks)
   persistent  1: one persistent launch per pass instead of the level
               launches (WG_BATCH_PERSISTENT), with persist_ctas CTAs per SM
+  adj_overlap 2: each size class's adjoint follows its own forward at the
+              class's stream priority; 1: at the lowest priority; 0: after
+              every class's forward (WG_ADJ_OVERLAP)
 
 ``tune(wm, ccds)`` builds the batch under candidate settings, times a few
 evaluations of each on the device (CUDA events around the launch sequence,
@@ -54,7 +57,7 @@ N_CLASSES = max(len(b) for b in CLASS_BOUNDS) + 1
 
 DEFAULTS: Dict[str, int] = {"target_ops": 480, "target_j": 3, "root_group": 16, "heavy_ops": 1024,
                             **{f"heavy_c{i}": 0 for i in range(N_CLASSES)},
-                            "classes": 0, "persistent": 0, "persist_ctas": 3}
+                            "classes": 0, "persistent": 0, "persist_ctas": 3, "adj_overlap": 2}
 NEIGHBOURS: Dict[str, Tuple[int, ...]] = {
     "target_ops": (240, 320, 480, 720, 960),
     "target_j": (2, 3, 4, 5),
@@ -63,10 +66,12 @@ NEIGHBOURS: Dict[str, Tuple[int, ...]] = {
     **{f"heavy_c{i}": (0, 256, 512, 2048, 1 << 20) for i in range(N_CLASSES)},
     "classes": tuple(range(len(CLASS_BOUNDS))),
     "persistent": (0, 1),
+    "adj_overlap": (0, 1, 2),
 }
 _ENV = {"target_ops": "WG_PACK_TARGET_OPS", "target_j": "WG_PACK_TARGET_J", "root_group": "WG_PACK_ROOT_GROUP",
         "heavy_ops": "WG_PACK_HEAVY_OPS", **{f"heavy_c{i}": f"WG_PACK_HEAVY_OPS_C{i}" for i in range(N_CLASSES)},
-        "classes": "WG_CLASS_BOUNDS", "persistent": None, "persist_ctas": "WG_PERSIST_CTAS"}
+        "classes": "WG_CLASS_BOUNDS", "persistent": None, "persist_ctas": "WG_PERSIST_CTAS",
+        "adj_overlap": "WG_ADJ_OVERLAP"}
 
 
 def _env_value(knob: str, v: int):
