@@ -312,7 +312,7 @@ def run_tune(args, W):
 
     wl = make_workload(synth, args.config, args.families, 0)
     wm, ccds = wl.model, wl.ccds()
-    nb = {"classes": tuple(range(len(autotune.CLASS_BOUNDS))), "persistent": (0, 1),
+    nb = {"classes": tuple(range(len(autotune.CLASS_BOUNDS))), "persistent": (0, 1), "adj_overlap": (0, 1, 2, 3),
           **{f"heavy_c{i}": (0, 512, 2048, 1 << 20) for i in range(autotune.N_CLASSES)},
           "target_ops": (320, 480, 720), "target_j": (2, 3, 4), "root_group": (8, 16, 32)}
     best, b, log = W.tune(wm, ccds, steps=max(3, args.steps), warmup=3, neighbours=nb, rounds=2)

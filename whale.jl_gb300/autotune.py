@@ -17,8 +17,8 @@ The packer's knobs decide how a batch maps onto the GPU:
   persistent  1: one persistent launch per pass instead of the level
               launches (WG_BATCH_PERSISTENT), with persist_ctas CTAs per SM
   adj_overlap 2: each size class's adjoint follows its own forward at the
-              class's stream priority; 1: at the lowest priority; 0: after
-              every class's forward (WG_ADJ_OVERLAP)
+              class's stream priority; 1 (3): at the lowest (highest)
+              priority; 0: after every class's forward (WG_ADJ_OVERLAP)
 
 ``tune(wm, ccds)`` builds the batch under candidate settings, times a few
 evaluations of each on the device (CUDA events around the launch sequence,
@@ -66,7 +66,7 @@ NEIGHBOURS: Dict[str, Tuple[int, ...]] = {
     **{f"heavy_c{i}": (0, 256, 512, 2048, 1 << 20) for i in range(N_CLASSES)},
     "classes": tuple(range(len(CLASS_BOUNDS))),
     "persistent": (0, 1),
-    "adj_overlap": (0, 1, 2),
+    "adj_overlap": (0, 1, 2, 3),
 }
 _ENV = {"target_ops": "WG_PACK_TARGET_OPS", "target_j": "WG_PACK_TARGET_J", "root_group": "WG_PACK_ROOT_GROUP",
         "heavy_ops": "WG_PACK_HEAVY_OPS", **{f"heavy_c{i}": f"WG_PACK_HEAVY_OPS_C{i}" for i in range(N_CLASSES)},

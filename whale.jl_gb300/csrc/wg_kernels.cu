@@ -1638,9 +1638,9 @@ struct wg_batch {
   int64_t tab_full = 0, tab_kept = 0;  // table doubles: every table / held on the device
   // 2 (default): each size class's adjoint follows its own forward on
   // streams of the class's priority, overlapping the other classes' forwards
-  // (1.62 against 1.66 ms per config-1 gradient evaluation); 1: the same at
-  // the lowest stream priority; 0: the adjoint starts once every class's
-  // forward is done (WG_ADJ_OVERLAP)
+  // (1.62 against 1.66 ms per config-1 gradient evaluation); 1 (3): the same
+  // at the lowest (highest) stream priority; 0: the adjoint starts once every
+  // class's forward is done (WG_ADJ_OVERLAP)
   int adj_overlap = 2;
   bool persist = false;                // persistent launches (WG_BATCH_PERSISTENT)
   int* d_err = nullptr;                // error bits of an evaluation: 1 dependency wait, 2 bulk-copy wait
@@ -1863,7 +1863,7 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
   // fits WG_PERSIST_CTAS (default 3) CTAs per SM; wider tasks keep their rows
   // in device memory
   b->persist = (flags & WG_BATCH_PERSISTENT) != 0;
-  b->adj_overlap = (int)pack_knob("WG_ADJ_OVERLAP", 2, 0, 2);
+  b->adj_overlap = (int)pack_knob("WG_ADJ_OVERLAP", 2, 0, 3);
   const int64_t pctas = pack_knob("WG_PERSIST_CTAS", 3, 1, 8);
   // (an SM's shared memory split over pctas CTAs, less the 1 KB the
   // hardware reserves per CTA and a margin for the kernels' static variables)
@@ -2054,7 +2054,7 @@ std::unique_ptr<wg_batch> build_batch(wg_ctx* ctx, const wg_model* m, wg_ccd* co
       ck(cudaStreamCreateWithPriority(&sb->s, cudaStreamNonBlocking, pr), "cudaStreamCreate");
       ck(cudaStreamCreateWithPriority(&sb->s2, cudaStreamNonBlocking, pr), "cudaStreamCreate");
       if (b->adj_overlap) {
-        const int pa = b->adj_overlap == 1 ? prio_lo : pr;
+        const int pa = b->adj_overlap == 1 ? prio_lo : b->adj_overlap == 3 ? prio_hi : pr;
         ck(cudaStreamCreateWithPriority(&sb->sa, cudaStreamNonBlocking, pa), "cudaStreamCreate");
         ck(cudaStreamCreateWithPriority(&sb->sa2, cudaStreamNonBlocking, pa), "cudaStreamCreate");
       }
