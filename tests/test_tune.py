@@ -73,13 +73,13 @@ def test_shape_knobs_reach_the_environment(W):
 
     from whale_gb300 import autotune as tune
 
-    with tune.packing({"classes": 1, "heavy_c2": 2048, "heavy_c3": 0, "persist_ctas": 4}):
-        assert os.environ["WG_CLASS_BOUNDS"] == ",".join(map(str, tune.CLASS_BOUNDS[1]))
+    with tune.packing({"classes": 2, "heavy_c2": 2048, "heavy_c3": 0, "persist_ctas": 4}):
+        assert os.environ["WG_CLASS_BOUNDS"] == ",".join(map(str, tune.CLASS_BOUNDS[2]))
         assert os.environ["WG_PACK_HEAVY_OPS_C2"] == "2048"
         assert "WG_PACK_HEAVY_OPS_C3" not in os.environ
         assert os.environ["WG_PERSIST_CTAS"] == "4"
     assert "WG_CLASS_BOUNDS" not in os.environ and "WG_PACK_HEAVY_OPS_C2" not in os.environ
-    sh = tune.shapes({"classes": 1, "heavy_ops": 1024, "heavy_c0": 256})
+    sh = tune.shapes({"classes": 2, "heavy_ops": 1024, "heavy_c0": 256})
     assert [x["clades"] for x in sh] == [(1, 128), (129, 512), (513, 1536), (1537, None)]
     assert sh[0]["heavy_ops"] == 256 and sh[1]["heavy_ops"] == 1024
     assert tune.shapes({"persistent": 1, "persist_ctas": 4})[0]["ctas_per_sm"] == 4

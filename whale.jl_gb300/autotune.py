@@ -47,6 +47,7 @@ from . import _native as N
 # size-class bounds (clade counts) the ``classes`` knob chooses from; the
 # first is the library's default
 CLASS_BOUNDS: Tuple[Tuple[int, ...], ...] = (
+    (192, 512, 1536),
     (128, 256, 512, 1024, 1536),
     (128, 512, 1536),
     (64, 128, 256, 512, 1024, 1536),

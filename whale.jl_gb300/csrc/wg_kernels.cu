@@ -1780,7 +1780,10 @@ KArgs plain_args(const PlainBatch* b) {
 // own and run on its own pair of streams: the levels of one class do not wait
 // for the levels of another.  Larger classes carry the critical paths and get
 // higher stream priorities, so their CTAs are dispatched first.
-constexpr int kClassBounds[] = {128, 256, 512, 1024, 1536, 1 << 30};
+// (192, 512, 1536): measured best of 13 bound sets on config 1 with each
+// class's adjoint on its own forward's heels (1.570 ms per gradient
+// evaluation against 1.615 ms for (128, 256, 512, 1024, 1536)).
+constexpr int kClassBounds[] = {192, 512, 1536, 1 << 30};
 
 // The size classes' upper bounds: WG_CLASS_BOUNDS (increasing clade counts,
 // comma-separated, at most 7; a last class takes the rest), else the above.
