@@ -156,7 +156,10 @@ int wg_ccd_export(const wg_ccd* c, int32_t* nleaves, int64_t* counts, int32_t* s
                   int32_t* species, int32_t* split_offsets, int32_t* split_g1, int32_t* split_g2,
                   double* split_p);
 
-/* ---- device-resident batch of families -------------------------------- */
+/* ---- device-resident batch of families --------------------------------
+ * The batch keeps pointers to its CCDs (wg_logpdf_plain and wg_track_device
+ * build their own layouts from them on first use): destroy the batch before
+ * its CCDs. */
 int wg_batch_create(wg_ctx* ctx, const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_t flags,
                     wg_batch** out);
 int wg_batch_destroy(wg_batch* b);
