@@ -312,6 +312,29 @@ __device__ __forceinline__ void prefetch_prog(const DEntry* __restrict__ E, cons
   if ((int)threadIdx.x < pr.ncomb) prefetch_l1(E + pr.comb + threadIdx.x);
 }
 
+// L2 prefetch of a root task's level programs: the same-row levels run one
+// after another with a barrier between them and each loads the next level's
+// entries, so a DRAM latency per level would otherwise sit on the chain.  The
+// levels' entries (lane entries then combine entries, level after level) and
+// their descriptors are each one contiguous range; warp 0 issues bulk L2
+// prefetches of 16 KB pieces of both.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+static_assert(sizeof(DEntry) == 16 && sizeof(DProg2) % 16 == 0, "bulk prefetch pieces are multiples of 16 bytes");
+__device__ __forceinline__ void prefetch_levels(const DEntry* __restrict__ E, const DProg2* __restrict__ progs, int nl) {
+  if (nl <= 0 || threadIdx.x >= 32) return;
+  constexpr int64_t kPiece = 16384;
+  const DProg2 a = progs[0], b = progs[nl - 1];
+  const char* lo = reinterpret_cast<const char*>(E + a.off);
+  const int64_t bytes = (b.comb + b.ncomb - a.off) * (int64_t)sizeof(DEntry);
+  for (int64_t o = (int64_t)threadIdx.x * kPiece; o < bytes; o += 32 * kPiece)
+    bulk_prefetch_l2(lo + o, (uint32_t)min(kPiece, bytes - o));
+  const int64_t dbytes = (int64_t)nl * (int64_t)sizeof(DProg2);
+  for (int64_t o = (int64_t)threadIdx.x * kPiece; o < dbytes; o += 32 * kPiece)
+    bulk_prefetch_l2(reinterpret_cast<const char*>(progs) + o, (uint32_t)min(kPiece, dbytes - o));
+}
+
 // General lane program: products accumulate, finalize ops call fin().
 // Entries are fetched four at a time ahead of their use.
 template <class Fin>
@@ -486,15 +509,43 @@ __device__ __forceinline__ void rows_reg(const LaneProg<MAXJ>& lp, const double*
   reg_steps<MAXJ, FIN>(lp, A, B, part, ph, ps, onfin, acc);
 }
 
+// A lane's first MAXJ entries of a level program as loaded (decoded where
+// they are used): the loads of the next level are issued while the current
+// one runs and nothing waits for them until that level starts.
+template <int MAXJ>
+struct LaneRaw {
+  ulonglong2 r[MAXJ];
+  int J;
+};
+template <int MAXJ>
+__device__ __forceinline__ void load_lane_raw(const DEntry* __restrict__ E, const DProg2& pr, int lane,
+                                              LaneRaw<MAXJ>& lr) {
+  lr.J = lane < pr.nt ? pr.J : 0;
+  const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + pr.off) + lane;
+#pragma unroll
+  for (int j = 0; j < MAXJ; ++j)
+    lr.r[j] = j < lr.J ? __ldg(e + (size_t)j * pr.nt) : make_ulonglong2(0, (uint64_t)op::NOP << 48);
+}
+template <int MAXJ, unsigned FIN, class OnFin>
+__device__ __forceinline__ void raw_steps(const LaneRaw<MAXJ>& lr, const double* A, const double* B, double* part,
+                                          double ph, double ps, OnFin& onfin, double& acc) {
+#pragma unroll
+  for (int j = 0; j < MAXJ; ++j)
+    if (j < lr.J) {
+      const Raw x = decode(lr.r[j]);
+      lane_step<FIN>(x.f0, x.f1, x.f2, x.opc, x.p, A, B, part, ph, ps, onfin, acc);
+    }
+}
+
 // The same-row levels of a root row (Πroot), run by the NTG threads of the
 // CTA for all the task's families in lock step: level after level with a
 // barrier between them; entries as in lane_step (products and the
 // finalize op FIN).  Levels are short and latency-bound, so each level's
-// first kLvlJ entries per lane, its first combine entry per thread and the
-// descriptor of the level after it are loaded while the level before it
-// runs; entries past kLvlJ are prefetched to L1 then.  comb(opc, c, fa, fb, s)
-// finishes split clades after a barrier.  wl: lane in the program, tix:
-// thread index among the NTG.
+// first kLvlJ entries per lane and its first combine entry per thread are
+// loaded while the level before it runs (held as loaded, decoded at use) and
+// the descriptor two levels ahead; entries past kLvlJ are prefetched to L1
+// then.  comb(opc, c, fa, fb, s) finishes split clades after a barrier.
+// wl: lane in the program, tix: thread index among the NTG.
 constexpr int kLvlJ = 4;
 template <int NTG, bool REVERSE, unsigned FIN, class OnFin, class Comb>
 __device__ __forceinline__ void chain_levels(const DEntry* __restrict__ E, const DProg2* __restrict__ progs, int nlvl,
@@ -508,16 +559,16 @@ __device__ __forceinline__ void chain_levels(const DEntry* __restrict__ E, const
   auto at = [&](int i) { return REVERSE ? nlvl - 1 - i : i; };
   DProg2 cur = progs[at(0)];
   DProg2 nxt = nlvl > 1 ? progs[at(1)] : cur;
-  LaneProg<kLvlJ> lp;
-  load_lane_prog<kLvlJ>(E, cur, wl, lp);
+  LaneRaw<kLvlJ> lp;
+  load_lane_raw<kLvlJ>(E, cur, wl, lp);
   CombReg cr = load_comb(E, cur, tix);
   for (int i = 0; i < nlvl; ++i) {
     const bool more = i + 1 < nlvl;
-    LaneProg<kLvlJ> lpn;
+    LaneRaw<kLvlJ> lpn;
     CombReg crn = cr;
     DProg2 nn = nxt;
     if (more) {
-      load_lane_prog<kLvlJ>(E, nxt, wl, lpn);
+      load_lane_raw<kLvlJ>(E, nxt, wl, lpn);
       crn = load_comb(E, nxt, tix);
       if (i + 2 < nlvl) nn = progs[at(i + 2)];
       if (wl < nxt.nt)  // the next level's entries past the registers, to L1
@@ -525,7 +576,7 @@ __device__ __forceinline__ void chain_levels(const DEntry* __restrict__ E, const
     }
     if (wl < cur.nt) {
       double acc = 0.0;
-      reg_steps<kLvlJ, FIN>(lp, A, B, part, ph, ps, onfin, acc);
+      raw_steps<kLvlJ, FIN>(lp, A, B, part, ph, ps, onfin, acc);
       const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + cur.off) + wl;
       for (int j = kLvlJ; j < cur.J; ++j) {
         const Raw x = decode(__ldg(e + (size_t)j * cur.nt));
@@ -674,6 +725,7 @@ __device__ __forceinline__ void fwd_task(const KArgs2& A, const DTask& T, int ro
       prefetch_l1(A.params + 2 * NR + roff + r);
     }
   } else {
+    prefetch_levels(E, A.progs + T.lvl, T.nlvl);
     prefetch_prog(E, T.init, lane);
   }
   if (!ROOT && mn.x == WG_NODE_LEAF) {
@@ -1116,6 +1168,7 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
       prefetch_l1(A.params + 2 * NR + roff + r);
     }
   } else {
+    prefetch_levels(E, A.progs + T.tlvl, T.nlvl);
     prefetch_prog(E, T.init, lane);
     prefetch_prog(E, T.ta, lane);
     prefetch_prog(E, T.tb, lane);
