@@ -274,7 +274,8 @@ struct DProg2 {
   int32_t nt = 0;       // lanes used (multiple of 32)
   int64_t comb = 0;     // combine entries (one per split clade)
   int32_t ncomb = 0;
-  int32_t nslot = 0;
+  uint16_t nslot = 0;   // partial slots (host: shared-memory sizing)
+  uint16_t nbig = 0;    // leading combine entries a warp each combines (the rest: a thread each)
 };
 
 struct DTask {
@@ -348,6 +349,11 @@ struct PackOptions2 {
   // device memory (L2-resident) instead
   int64_t smem_limit_doubles = 227 * 1024 / 8;
   int target_j = (int)pack_knob("WG_PACK_TARGET_J", 3, 1, 16);  // iterations per row the lane scheduler aims for
+  // split clades of the forward programs with at least this many partial
+  // sums are combined by a warp each (0: every one by a thread; adjoint
+  // programs always combine by thread).  Measured on 5,000 config-1
+  // families: 24 gives 1.510 ms per gradient evaluation, 0 1.517 ms.
+  int comb_warp = (int)pack_knob("WG_PACK_COMB_WARP", 24, 0, 1 << 16);
   // persistent launches: every task takes kNT2L threads, and a root task's
   // families are grouped so that its adjoint rows fit in this many shared
   // doubles (0: no such bound)

@@ -380,16 +380,47 @@ __device__ __forceinline__ void comb_one(const ulonglong2 raw, const double* par
   fin(x.opc, x.f0, x.f1, x.f2, s + t);
 }
 
-// Combine pass for split clades (one thread per clade).
-template <int NT, class Fin>
+// The first pr.nbig combine entries (split clades with many partial sums):
+// one warp each, lanes summing strided partials (two chains), then
+// a shuffle tree; lane 0 hands the sum to fin().  tix: the thread's index
+// among the NTG threads that share the pass.
+template <int NTG, class Fin>
+__device__ __forceinline__ void comb_big(const DEntry* __restrict__ E, const DProg2& pr, const double* part, Fin& fin,
+                                         int tix) {
+  const int l = tix & 31;
+  for (int i = tix >> 5; i < (int)pr.nbig; i += NTG / 32) {
+    const ulonglong2 raw = __ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + i));
+    const unsigned s0 = (unsigned)(raw.y & 0xFFFFFFFFu), n = (unsigned)(raw.y >> 32);
+    double s = 0.0, t = 0.0;
+    unsigned k = (unsigned)l;
+    for (; k + 32 < n; k += 64) {
+      s += part[s0 + k];
+      t += part[s0 + k + 32];
+    }
+    if (k < n) s += part[s0 + k];
+    s += t;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (l == 0) {
+      const Raw x = decode(raw);
+      fin(x.opc, x.f0, x.f1, x.f2, s);
+    }
+  }
+}
+
+// Combine pass for split clades: with BIG the first pr.nbig a warp each,
+// the rest one thread each.  (Adjoint programs have no warp-combined
+// entries: their passes leave the warp code out of the row loops.)
+template <int NT, bool BIG, class Fin>
 __device__ __forceinline__ void run_comb(const DEntry* __restrict__ E, const DProg2& pr, const double* part,
                                          Fin fin) {
-  for (int i = threadIdx.x; i < pr.ncomb; i += NT)
+  if constexpr (BIG) comb_big<NT>(E, pr, part, fin, (int)threadIdx.x);
+  for (int i = pr.nbig + threadIdx.x; i < pr.ncomb; i += NT)
     comb_one(__ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + i)), part, fin);
 }
 
-// A thread's first combine entry of a program, held in registers while the
-// program repeats (rows of a branch) or runs later (next root level).
+// A thread's first one-thread combine entry of a program, held in registers
+// while the program repeats (rows of a branch) or runs later (next root
+// level).
 struct CombReg {
   ulonglong2 raw;
 };
@@ -397,14 +428,17 @@ struct CombReg {
 __device__ __forceinline__ CombReg load_comb(const DEntry* __restrict__ E, const DProg2& pr,
                                              int tix = (int)threadIdx.x) {
   CombReg c;
-  c.raw = tix < pr.ncomb ? __ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + tix)) : make_ulonglong2(0, 0);
+  const int i = pr.nbig + tix;
+  c.raw = i < pr.ncomb ? __ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + i)) : make_ulonglong2(0, 0);
   return c;
 }
-template <int NT, class Fin>
+template <int NT, bool BIG, class Fin>
 __device__ __forceinline__ void run_comb_reg(const DEntry* __restrict__ E, const DProg2& pr, const CombReg& cr,
                                              const double* part, Fin fin, int tix = (int)threadIdx.x) {
-  if (tix < pr.ncomb) comb_one(cr.raw, part, fin);
-  for (int i = tix + NT; i < pr.ncomb; i += NT)
+  if constexpr (BIG) comb_big<NT>(E, pr, part, fin, tix);
+  const int i0 = pr.nbig + tix;
+  if (i0 < pr.ncomb) comb_one(cr.raw, part, fin);
+  for (int i = i0 + NT; i < pr.ncomb; i += NT)
     comb_one(__ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + i)), part, fin);
 }
 
@@ -585,7 +619,7 @@ __device__ __forceinline__ void chain_levels(const DEntry* __restrict__ E, const
     }
     if (cur.ncomb) {
       sync();
-      run_comb_reg<NTG>(E, cur, cr, part, comb, tix);
+      run_comb_reg<NTG, !REVERSE>(E, cur, cr, part, comb, tix);
     }
     sync();
     if (more) {
@@ -625,7 +659,7 @@ __device__ __forceinline__ void fwd_rows(const DEntry* __restrict__ E, const DTa
     if (dup.ncomb) {
       __syncthreads();
       const double* cc = cur;
-      run_comb_reg<NT>(E, dup, cr, part, [&](unsigned, unsigned c, unsigned, unsigned, double s) {
+      run_comb_reg<NT, true>(E, dup, cr, part, [&](unsigned, unsigned c, unsigned, unsigned, double s) {
         const double v = fma(ps, s, ph * cc[c]);
         o[c] = v;
         if (TABLES) tr[c] = v;
@@ -652,7 +686,7 @@ __device__ __forceinline__ void fwd_rows_generic(const DEntry* __restrict__ E, c
       __syncthreads();
       const double* cc = cur;
       double* o = nxt;
-      run_comb_reg<NT>(E, dup, cr, part, [&](unsigned, unsigned c, unsigned, unsigned, double s) {
+      run_comb_reg<NT, true>(E, dup, cr, part, [&](unsigned, unsigned c, unsigned, unsigned, double s) {
         const double v = fma(ps, s, ph * cc[c]);
         o[c] = v;
         if (TABLES) tr[c] = v;
@@ -699,6 +733,24 @@ __device__ __forceinline__ double ld_shared_row(const double* p) {
   else return *p;
 }
 
+// dst[i] = src[gm[i]] for i < n over the CTA's NT threads: each gather is two
+// dependent global loads, so every thread has four indices and then four
+// values in flight at a time rather than one of each.
+template <int NT, bool CG>
+__device__ __forceinline__ void gather_rows(double* dst, const double* src, const int64_t* __restrict__ gm, int n) {
+  for (int i0 = (int)threadIdx.x; i0 < n; i0 += 4 * NT) {
+    int64_t g[4];
+    double v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) g[u] = i0 + u * NT < n ? __ldg(gm + i0 + u * NT) : 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = i0 + u * NT < n ? ld_shared_row<CG>(src + g[u]) : 0.0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (i0 + u * NT < n) dst[i0 + u * NT] = v[u];
+  }
+}
+
 // One forward task (one species node for a group of families).  rot rotates
 // the lane assignment by warps (spreads the lanes' programs over the warps of
 // successive CTAs); CG: the children's top rows were written in this launch.
@@ -734,7 +786,7 @@ __device__ __forceinline__ void fwd_task(const KArgs2& A, const DTask& T, int ro
     for (int c = tid; c < R; c += NT) cur[c] = aux[c] ? lp : 0.0;
   } else {
     const int64_t* gm = A.gmap + T.gmap;
-    for (int i = tid; i < T.wa + T.wb; i += NT) nxt[i] = ld_shared_row<CG>(A.tops + gm[i]);
+    gather_rows<NT, CG>(nxt, A.tops, gm, T.wa + T.wb);
     __syncthreads();
     const double* X = nxt;
     const double* Y = nxt + T.wa;
@@ -748,7 +800,7 @@ __device__ __forceinline__ void fwd_task(const KArgs2& A, const DTask& T, int ro
       run_any(E, T.init, lane, X, X, part, fin);
       if (T.init.ncomb) {
         __syncthreads();
-        run_comb<NT>(E, T.init, part, fin);
+        run_comb<NT, true>(E, T.init, part, fin);
       }
     } else {
       const double ea = eps_top2(A, mn.y), eb = eps_top2(A, mn.z);
@@ -760,7 +812,7 @@ __device__ __forceinline__ void fwd_task(const KArgs2& A, const DTask& T, int ro
       run_any(E, T.init, lane, X, Y, part, fin);
       if (T.init.ncomb) {
         __syncthreads();
-        run_comb<NT>(E, T.init, part, fin);
+        run_comb<NT, true>(E, T.init, part, fin);
       }
       if (ROOT) {
         // whaleroot! (src/core.jl:130-149), Πroot over smaller clades of the
@@ -1018,7 +1070,7 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
     if (td.ncomb) {
       __syncthreads();
       // (combine entries stream from memory here: registers are the limit)
-      run_comb<NT>(E, td, part, [&](unsigned, unsigned c, unsigned, unsigned, double g) {
+      run_comb<NT, false>(E, td, part, [&](unsigned, unsigned c, unsigned, unsigned, double g) {
         bn[c] = fma(ps, g, ph * bb[c]);
         if constexpr (!ONEDOT) Gs[c] = g;
       });
@@ -1206,7 +1258,7 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
     // stage the children's tops, recompute Πspec + Πloss for ∂/∂cb
     double* X = barn;
     double* Y = barn + T.wa;
-    for (int i = tid; i < T.wa + T.wb; i += NT) barn[i] = A.tops[gm[i]];
+    gather_rows<NT, false>(barn, A.tops, gm, T.wa + T.wb);
     __syncthreads();
     const double ea = eps_top2(A, mn.y), eb = eps_top2(A, mn.z);
     double* bbc = L1;  // cb · bar, the adjoint of Πspec + Πloss
@@ -1220,7 +1272,7 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
     run_any(E, T.init, lane, X, Y, part, sfin);
     if (T.init.ncomb) {
       __syncthreads();
-      run_comb<NT>(E, T.init, part, sfin);
+      run_comb<NT, true>(E, T.init, part, sfin);
     }
     for (int c = tid; c < R; c += NT) {
       const double b = cb * bar[c];
@@ -1241,8 +1293,8 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
     run_any(E, T.tb, lane, bbc, X, part, bfin);
     if (T.ta.ncomb || T.tb.ncomb) {
       __syncthreads();
-      run_comb<NT>(E, T.ta, part, afin);
-      run_comb<NT>(E, T.tb, part, bfin);
+      run_comb<NT, false>(E, T.ta, part, afin);
+      run_comb<NT, false>(E, T.tb, part, bfin);
     }
     block_sum4<NT>(acc4, red);
     if (tid == 0) {
@@ -1289,7 +1341,7 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
   // ---- row 0
   if (mn.x == WG_NODE_WGD) {
     double* X = L0;
-    for (int i = tid; i < T.wa; i += NT) X[i] = A.tops[gm[i]];
+    gather_rows<NT, false>(X, A.tops, gm, T.wa);
     __syncthreads();
     const double q = A.params[3 * NR + k];
     const double ef = eps_top2(A, mn.y);
@@ -1314,7 +1366,7 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
     }
     if (T.tdup.ncomb) {
       __syncthreads();
-      run_comb<NT>(E, T.tdup, part, wfin);
+      run_comb<NT, false>(E, T.tdup, part, wfin);
     }
     block_sum4<NT>(acc4, red);
     if (tid == 0) {
@@ -1324,7 +1376,7 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
   } else if (mn.x == WG_NODE_INTERNAL) {
     double* X = L0;
     double* Y = L0 + T.wa;
-    for (int i = tid; i < T.wa + T.wb; i += NT) L0[i] = A.tops[gm[i]];
+    gather_rows<NT, false>(L0, A.tops, gm, T.wa + T.wb);
     __syncthreads();
     const double ea = eps_top2(A, mn.y), eb = eps_top2(A, mn.z);
     auto afin = [&](unsigned, unsigned x, unsigned fa, unsigned, double acc) {
@@ -1338,8 +1390,8 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
     run_any(E, T.tb, lane, bar, X, part, bfin);
     if (T.ta.ncomb || T.tb.ncomb) {
       __syncthreads();
-      run_comb<NT>(E, T.ta, part, afin);
-      run_comb<NT>(E, T.tb, part, bfin);
+      run_comb<NT, false>(E, T.ta, part, afin);
+      run_comb<NT, false>(E, T.tb, part, bfin);
     }
     double acc4[4] = {0.0, 0.0, 0.0, 0.0};  // dea, deb
     const int2* loss = reinterpret_cast<const int2*>(A.meta) + T.loss;

@@ -598,7 +598,8 @@ inline int first_set(const uint64_t* w, int nw) {
 // room for them (first-fit decreasing into lanes of J ops); J grows until
 // they fit.  Partial slots are numbered from slot_base (a program run right
 // after another without a barrier takes slots after the other's).
-DProg2 schedule2(const ItemList& items, int ntmax, int target_j, EntryBuf& out, int slot_base = 0) {
+DProg2 schedule2(const ItemList& items, int ntmax, int target_j, EntryBuf& out, int slot_base = 0,
+                 int comb_warp = 0) {
   DProg2 pr;
   pr.off = (int64_t)out.size();
   const int n = items.size();
@@ -710,10 +711,21 @@ DProg2 schedule2(const ItemList& items, int ntmax, int target_j, EntryBuf& out, 
     }
     for (; j < J; ++j) base[(size_t)j * nt + t] = nop;
   }
-  // combine entries
+  // combine entries (with comb_warp: largest first, the first nbig, those
+  // of at least comb_warp partial sums, combined by a warp each); the rest
+  // are combined by a thread each
   pr.comb = (int64_t)out.size();
-  for (int i = 0; i < n; ++i) {
-    if (nseg[i] <= 1) continue;
+  std::vector<int> cs;
+  for (int i = 0; i < n; ++i)
+    if (nseg[i] > 1) cs.push_back(i);
+  int nbig = 0;
+  if (comb_warp > 0) {
+    std::stable_sort(cs.begin(), cs.end(), [&](int x, int y) { return nseg[x] > nseg[y]; });
+    while (nbig < (int)cs.size() && nseg[cs[nbig]] >= comb_warp) ++nbig;
+  }
+  if (nbig > 65535) throw Error(WG_ERANGE, "program exceeds 65535 combine entries");
+  pr.nbig = (uint16_t)nbig;
+  for (int i : cs) {
     const Item& it = items.items[i];
     const uint64_t sl = (uint64_t)(uint32_t)slot0[i] | ((uint64_t)(uint32_t)nseg[i] << 32);
     out.push_back(DEntry{pack_code(it.c, it.fa, it.fb, it.fin), bits_to_double(sl)});
@@ -903,7 +915,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
             items.close();
           }
         }
-        if (has_rows) T.dup = schedule2(items, NT, opt.target_j, entries);
+        if (has_rows) T.dup = schedule2(items, NT, opt.target_j, entries, 0, opt.comb_warp);
         if (opt.adjoint) T.tdup = schedule2(titems.finish(), NT, opt.target_j, entries);
       }
       if (kind == WG_NODE_LEAF) {
@@ -931,7 +943,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
             items.close();
           }
         }
-        T.init = schedule2(items, NT, opt.target_j, entries);
+        T.init = schedule2(items, NT, opt.target_j, entries, 0, opt.comb_warp);
       } else {
         // speciation + loss (internal) or Πspec + Πloss of the root row
         ItemList items;
@@ -966,7 +978,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
             items.close();
           }
         }
-        T.init = schedule2(items, NT, opt.target_j, entries);
+        T.init = schedule2(items, NT, opt.target_j, entries, 0, opt.comb_warp);
         T.loss = put_int2(meta, loss);
         if (opt.adjoint) {
           for (int x = 0; x < T.wa; ++x) ta.items[x].fa = inva[x] < 0 ? 0xFFFF : inva[x];
@@ -1018,12 +1030,13 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
         }
         T.nlvl = nl;
         T.lvl = (int64_t)tb.progs.size();
-        for (int L = 0; L < nl; ++L) tb.progs.push_back(schedule2(lw[L], NT, opt.target_j, entries));
+        for (int L = 0; L < nl; ++L)
+          tb.progs.push_back(schedule2(lw[L], NT, opt.target_j, entries, 0, opt.comb_warp));
         if (opt.adjoint) {
           T.tlvl = (int64_t)tb.progs.size();
           for (int L = 0; L < nl; ++L) tb.progs.push_back(schedule2(tlw[L], NT, opt.target_j, entries));
         }
-        for (const DProg2& q : tb.progs) T.rslot = std::max(T.rslot, q.nslot);
+        for (const DProg2& q : tb.progs) T.rslot = std::max(T.rslot, (int32_t)q.nslot);
       }
       if (kind == WG_NODE_ROOT) {
         // log L outputs: family index and position of its ubiquitous clade
@@ -1033,7 +1046,7 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
         T.fam = put_int2(meta, fam);
       }
       // shared memory: cur + nxt rows (children staged in nxt) + slots + spare
-      int slots = std::max({T.dup.nslot, T.init.nslot, T.tdup.nslot, T.ta.nslot + T.tb.nslot});
+      int slots = std::max({(int)T.dup.nslot, (int)T.init.nslot, (int)T.tdup.nslot, T.ta.nslot + T.tb.nslot});
       slots = std::max(slots, T.rslot);  // root: the level programs' partial slots
       // forward: cur, nxt (children staged in nxt); adjoint: bar, barn, two
       // L rows, G; then partial slots and reduction scratch
