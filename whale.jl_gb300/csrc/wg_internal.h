@@ -252,6 +252,15 @@ Packed pack_batch(const Model& m, const std::vector<const CCD*>& ccds, const Pac
 // value; clades too long for one lane are split into partial slots that a
 // short combine pass (after one barrier) finishes.
 // ---------------------------------------------------------------------------
+// Kind of a program column (bits 56-63 of an entry's code), the same for the
+// 32 lanes of a warp: PROD columns hold products (or idle lanes), FIN columns
+// finalize ops (or partial-sum stores, or idle lanes), PART columns only
+// partial-sum stores, NOP columns nothing.  A warp then never runs two FP64
+// paths for one column.
+namespace col {
+enum : uint32_t { NOP = 0, PROD = 1, FIN = 2, PART = 3 };
+}
+
 namespace op {
 enum : uint32_t {
   PROD = 0,

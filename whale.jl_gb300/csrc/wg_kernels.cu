@@ -245,7 +245,7 @@ struct KArgs2 {
 };
 
 struct Raw {
-  unsigned f0, f1, f2, opc;
+  unsigned f0, f1, f2, opc, kind;
   double p;
 };
 
@@ -255,6 +255,7 @@ __device__ __forceinline__ Raw decode(const ulonglong2 r) {
   x.f1 = (unsigned)((r.x >> 16) & 0xFFFFu);
   x.f2 = (unsigned)((r.x >> 32) & 0xFFFFu);
   x.opc = (unsigned)((r.x >> 48) & 0xFFu);
+  x.kind = (unsigned)(r.x >> 56);
   x.p = __longlong_as_double((long long)r.y);
   return x;
 }
@@ -442,9 +443,32 @@ __device__ __forceinline__ void run_comb_reg(const DEntry* __restrict__ E, const
     comb_one(__ldg(reinterpret_cast<const ulonglong2*>(E + pr.comb + i)), part, fin);
 }
 
-// Row program of the branch recursion (PROD / FIN_DUP / FIN_PART): one DMUL and
-// one DFMA per entry whatever the op, operands routed by selects, so lanes of
-// a warp never split the FP64 instruction stream.
+// One entry of a lane program, by its column's kind (the same for the warp's
+// 32 lanes, so a warp takes one branch).  PROD column: acc = fma(p·A[f0],
+// B[f1], acc) on lanes holding a product (idle lanes keep acc); FIN column:
+// the finalize op FIN (entries with f0 = f1 = c) v = fma(ψ, acc, ϕ·A[c]),
+// handed to onfin(c, v, acc), or FIN_PART part[f2] = acc; PART column:
+// partial sums only.  Every finalize column clears acc.
+template <unsigned FIN, class OnFin>
+__device__ __forceinline__ void lane_step(unsigned kind, unsigned f0, unsigned f1, unsigned f2, unsigned opc,
+                                          double p, const double* A, const double* B, double* part, double ph,
+                                          double ps, OnFin& onfin, double& acc) {
+  if (kind == col::PROD) {
+    const double v = fma(p * A[f0], B[f1], acc);
+    acc = opc == op::PROD ? v : acc;
+  } else if (kind == col::FIN) {
+    const double v = fma(ps, acc, ph * A[f0]);
+    if (opc == FIN) onfin(f0, v, acc);
+    else if (opc == op::FIN_PART) part[f2] = acc;
+    acc = 0.0;
+  } else if (kind == col::PART) {
+    if (opc == op::FIN_PART) part[f2] = acc;
+    acc = 0.0;
+  }
+}
+
+// Row program of the branch recursion streamed from memory (programs deeper
+// than the register-resident instantiations): entries as in lane_step.
 //   PROD:    acc = fma(p·cur[a], cur[b], acc)
 //   FIN_DUP: out[c] = fma(ψ, acc, ϕ·cur[c])     (entry has a = b = c)
 template <bool STORE>
@@ -452,22 +476,14 @@ __device__ __forceinline__ void run_rows(const DEntry* __restrict__ E, const DPr
                                          double* out, double* part, double ph, double ps, double* tab) {
   if (lane >= pr.nt) return;
   const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + pr.off) + lane;
+  auto onfin = [&](unsigned c, double v, double) {
+    out[c] = v;
+    if (STORE) tab[c] = v;
+  };
   double acc = 0.0;
   for (int j = 0; j < pr.J; ++j, e += pr.nt) {
     const Raw x = decode(__ldg(e));
-    const bool fin = x.opc == op::FIN_DUP;
-    const double m = (fin ? ph : x.p) * cur[x.f0];
-    const double r = fma(fin ? ps : m, fin ? acc : cur[x.f1], fin ? m : acc);
-    if (x.opc == op::PROD) {
-      acc = r;
-    } else if (fin) {
-      out[x.f0] = r;
-      if (STORE) tab[x.f0] = r;
-      acc = 0.0;
-    } else if (x.opc == op::FIN_PART) {
-      part[x.f2] = acc;
-      acc = 0.0;
-    }
+    lane_step<op::FIN_DUP>(x.kind, x.f0, x.f1, x.f2, x.opc, x.p, cur, cur, part, ph, ps, onfin, acc);
   }
 }
 
@@ -492,35 +508,14 @@ __device__ __forceinline__ void load_lane_prog(const DEntry* __restrict__ E, con
     if (j < lp.J) {
       const ulonglong2 r = __ldg(e + (size_t)j * pr.nt);
       lp.ab[j] = (uint32_t)(r.x & 0xFFFFFFFFu);
-      lp.om[j] = (uint32_t)((r.x >> 32) & 0xFFFFu) | ((uint32_t)((r.x >> 48) & 0xFFu) << 16);
+      lp.om[j] = (uint32_t)((r.x >> 32) & 0xFFFFu) | ((uint32_t)((r.x >> 48) & 0xFFu) << 16) |
+                 ((uint32_t)(r.x >> 56) << 24);
       lp.p[j] = __longlong_as_double((long long)r.y);
     } else {
       lp.ab[j] = 0;
-      lp.om[j] = (uint32_t)op::NOP << 16;
+      lp.om[j] = (uint32_t)op::NOP << 16 | (uint32_t)col::NOP << 24;
       lp.p[j] = 0.0;
     }
-  }
-}
-
-// One entry of a lane program.  PROD: acc = fma(p·A[f0], B[f1], acc); the
-// finalize op FIN (entries with f0 = f1 = c): v = fma(ψ, acc, ϕ·A[c]),
-// handed to onfin(c, v, acc); FIN_PART: part[f2] = acc.  One DMUL and one
-// DFMA whatever the op, operands routed by selects.
-template <unsigned FIN, class OnFin>
-__device__ __forceinline__ void lane_step(unsigned f0, unsigned f1, unsigned f2, unsigned opc, double p,
-                                          const double* A, const double* B, double* part, double ph, double ps,
-                                          OnFin& onfin, double& acc) {
-  const bool fin = opc == FIN;
-  const double m = (fin ? ph : p) * A[f0];
-  const double v = fma(fin ? ps : m, fin ? acc : B[f1], fin ? m : acc);
-  if (opc == op::PROD) {
-    acc = v;
-  } else if (fin) {
-    onfin(f0, v, acc);
-    acc = 0.0;
-  } else if (opc == op::FIN_PART) {
-    part[f2] = acc;
-    acc = 0.0;
   }
 }
 
@@ -531,8 +526,8 @@ __device__ __forceinline__ void reg_steps(const LaneProg<MAXJ>& lp, const double
 #pragma unroll
   for (int j = 0; j < MAXJ; ++j)
     if (j < lp.J)
-      lane_step<FIN>(lp.ab[j] & 0xFFFFu, lp.ab[j] >> 16, lp.om[j] & 0xFFFFu, lp.om[j] >> 16, lp.p[j], A, B, part, ph,
-                     ps, onfin, acc);
+      lane_step<FIN>(lp.om[j] >> 24, lp.ab[j] & 0xFFFFu, lp.ab[j] >> 16, lp.om[j] & 0xFFFFu, (lp.om[j] >> 16) & 0xFFu,
+                     lp.p[j], A, B, part, ph, ps, onfin, acc);
 }
 
 // One row from a register-resident program.
@@ -567,7 +562,7 @@ __device__ __forceinline__ void raw_steps(const LaneRaw<MAXJ>& lr, const double*
   for (int j = 0; j < MAXJ; ++j)
     if (j < lr.J) {
       const Raw x = decode(lr.r[j]);
-      lane_step<FIN>(x.f0, x.f1, x.f2, x.opc, x.p, A, B, part, ph, ps, onfin, acc);
+      lane_step<FIN>(x.kind, x.f0, x.f1, x.f2, x.opc, x.p, A, B, part, ph, ps, onfin, acc);
     }
 }
 
@@ -614,7 +609,7 @@ __device__ __forceinline__ void chain_levels(const DEntry* __restrict__ E, const
       const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + cur.off) + wl;
       for (int j = kLvlJ; j < cur.J; ++j) {
         const Raw x = decode(__ldg(e + (size_t)j * cur.nt));
-        lane_step<FIN>(x.f0, x.f1, x.f2, x.opc, x.p, A, B, part, ph, ps, onfin, acc);
+        lane_step<FIN>(x.kind, x.f0, x.f1, x.f2, x.opc, x.p, A, B, part, ph, ps, onfin, acc);
       }
     }
     if (cur.ncomb) {
@@ -979,7 +974,7 @@ __device__ __forceinline__ void block_sum4(double (&v)[4], double* red) {
 // entries streamed) and write ∂/∂ϕ_r, ∂/∂ψ_r to out[2r], out[2r + 1].
 // GMEM: the task's rows live in device memory (plain copies, no bulk copies).
 // Otherwise each table row goes to its shared buffer as one 1-D bulk copy
-// (TMA) issued by thread 0 and completed on that buffer's mbarrier (mb[3]).
+// (TMA) issued by thread 0 and completed on that buffer's mbarrier (mb[NB]).
 template <int NT, int J, bool ONEDOT, bool GMEM>
 __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTask& T, int lane, int n, int R,
                                          const double* phs, const double* pss, double*& bar, double*& barn,
@@ -994,17 +989,20 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
   LaneProg<(J > 0 ? J : 1)> lp;
   if (J > 0) load_lane_prog<(J > 0 ? J : 1)>(E, td, lane, lp);
   const bool active = lane < td.nt;
+  // table-row buffers: four (copies three rows ahead) in the one-dot form,
+  // which leaves G unused and takes its row as the fourth; three otherwise
+  constexpr int NB = ONEDOT ? 4 : 3;
   if constexpr (!GMEM) {
     // the buffers may hold what generic stores left (an earlier task's rows)
     fence_proxy_async_smem();
     if (tid == 0) {
-      for (int i = 0; i < 3; ++i) mbar_init(mb + i);
+      for (int i = 0; i < NB; ++i) mbar_init(mb + i);
       mbar_init_fence();
     }
     __syncthreads();
   }
-  // Row r reads table row r-1 from buffer (n-1-r) mod 3 (buffer i at Lb +
-  // i·W2); the copies run two rows ahead (none past row 1).  par: bit i is
+  // Row r reads table row r-1 from buffer (n-1-r) mod NB (buffer i at Lb +
+  // i·W2); the copies run NB-1 rows ahead (none past row 1).  par: bit i is
   // the phase parity of buffer i's next completion.
   unsigned par = 0;
   auto fetch = [&](int rr, int buf) {
@@ -1050,21 +1048,13 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
     } else if (active) {
       const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + td.off) + lane;
       double acc = 0.0;
+      auto onfin = [&](unsigned c, double v, double g) {
+        bn[c] = v;
+        if constexpr (!ONEDOT) Gs[c] = g;
+      };
       for (int j = 0; j < td.J; ++j, e += td.nt) {
         const Raw x = decode(__ldg(e));
-        const bool fin = x.opc == op::FIN_ADJ;
-        const double m = (fin ? ph : x.p) * bb[x.f0];
-        const double v = fma(fin ? ps : m, fin ? acc : Lp[x.f1], fin ? m : acc);
-        if (x.opc == op::PROD) {
-          acc = v;
-        } else if (fin) {
-          bn[x.f0] = v;
-          if constexpr (!ONEDOT) Gs[x.f0] = acc;
-          acc = 0.0;
-        } else if (x.opc == op::FIN_PART) {
-          part[x.f2] = acc;
-          acc = 0.0;
-        }
+        lane_step<op::FIN_ADJ>(x.kind, x.f0, x.f1, x.f2, x.opc, x.p, bb, Lp, part, ph, ps, onfin, acc);
       }
     }
     if (td.ncomb) {
@@ -1077,24 +1067,23 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
     }
   };
   int bi = 0;
-  fetch(n - 1, 0);
-  fetch(n - 2, 1);
+  for (int i = 0; i + 1 < NB; ++i) fetch(n - 1 - i, i);
   if constexpr (ONEDOT) {
     // One CTA barrier per row: it follows the program (bar_{r-1} complete)
     // once the next row's table row has landed.  The dot reads only
     // bar_{r-1} and row r-1, which the next program does not write, and a
     // buffer is refilled only after the barrier that follows its last reader
-    // (the dot of the row above).
+    // (the dot of the row above: row r+1's buffer takes table row r-NB).
     landed(0);
     __syncthreads();
     for (int r = n - 1; r >= 1; --r) {
       double* Lp = Lb + bi * W2;
       double* bn = barn;
       row(r, Lp, bar, bn);
-      if (r >= 2) landed(bi == 2 ? 0 : bi + 1);
+      if (r >= 2) landed(bi + 1 == NB ? 0 : bi + 1);
       __syncthreads();
-      fetch(r - 2, bi == 0 ? 2 : bi - 1);  // row r+1's buffer takes table row r-3
-      bi = bi == 2 ? 0 : bi + 1;
+      fetch(r - (NB - 1), bi == 0 ? NB - 1 : bi - 1);
+      bi = bi + 1 == NB ? 0 : bi + 1;
       const int slot = (n - 1 - r) & 7;
       double e = 0.0;  // this lane's share of E_{r-1}
       for (int c = tid; c < R; c += NT) e = fma(bn[c], Lp[c], e);
@@ -1122,9 +1111,9 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
       double* Lp = Lb + bi * W2;
       landed(bi);
       __syncthreads();
-      // every thread is past row r+1, whose buffer takes table row r-3
-      fetch(r - 2, bi == 0 ? 2 : bi - 1);
-      bi = bi == 2 ? 0 : bi + 1;
+      // every thread is past row r+1, whose buffer takes table row r-NB
+      fetch(r - (NB - 1), bi == 0 ? NB - 1 : bi - 1);
+      bi = bi + 1 == NB ? 0 : bi + 1;
       const double* bb = bar;
       row(r, Lp, bb, barn);
       __syncthreads();
@@ -1163,7 +1152,7 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
   if constexpr (!GMEM) {  // every copy was waited for; row 0 reuses the buffers
     __syncthreads();
     if (tid == 0)
-      for (int i = 0; i < 3; ++i) mbar_inval(mb + i);
+      for (int i = 0; i < NB; ++i) mbar_inval(mb + i);
   }
 }
 
@@ -1328,7 +1317,7 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
     // one-dot row adjoints unless a row's ψ is tiny (uniform over the CTA)
     bool ok = true;
     for (int r = 1 + tid; r < n; r += NT) ok &= pss[r] >= kPsiOneDot && phs[r] > 0.0;
-    __shared__ __align__(8) uint64_t mb[3];  // the table-row buffers' mbarriers
+    __shared__ __align__(8) uint64_t mb[4];  // the table-row buffers' mbarriers
     if (!__syncthreads_and(ok))
       adj_rows<NT, 0, false, GLOBAL>(E, T, lane, n, R, phs, pss, bar, barn, L0, W2, Gs, part, red, tab0, out, mb,
                                      A.err);

@@ -574,9 +574,9 @@ struct ScatterList {
   }
 };
 
-inline uint64_t pack_code(uint32_t f0, uint32_t f1, uint32_t f2, uint32_t opc) {
+inline uint64_t pack_code(uint32_t f0, uint32_t f1, uint32_t f2, uint32_t opc, uint32_t kind = col::NOP) {
   return (uint64_t)(f0 & 0xFFFFu) | ((uint64_t)(f1 & 0xFFFFu) << 16) | ((uint64_t)(f2 & 0xFFFFu) << 32) |
-         ((uint64_t)opc << 48);
+         ((uint64_t)opc << 48) | ((uint64_t)kind << 56);
 }
 
 inline double bits_to_double(uint64_t b) {
@@ -594,10 +594,13 @@ inline int first_set(const uint64_t* w, int nw) {
 // Lane programs with fused finalize.  An item (one clade) is its products
 // followed by its finalize op; items longer than J ops are split into
 // segments ending in FIN_PART, finished by a combine entry after a barrier.
-// Segments go longest first (ties in item order) to the first lane with
-// room for them (first-fit decreasing into lanes of J ops); J grows until
-// they fit.  Partial slots are numbered from slot_base (a program run right
-// after another without a barrier takes slots after the other's).
+// The columns of a warp are uniform (col::): segments go longest first (ties
+// in item order) in bundles of 32, one per lane, each bundle as high as its
+// longest segment with every segment ending in the bundle's last column
+// (shorter ones start later; their lanes idle before); bundles stack in the
+// warps first-fit (J ops per lane); J grows until they fit.  Partial slots
+// are numbered from slot_base (a program run right after another without a
+// barrier takes slots after the other's).
 DProg2 schedule2(const ItemList& items, int ntmax, int target_j, EntryBuf& out, int slot_base = 0,
                  int comb_warp = 0) {
   DProg2 pr;
@@ -613,15 +616,11 @@ DProg2 schedule2(const ItemList& items, int ntmax, int target_j, EntryBuf& out, 
   // rows are latency-bound: enough warps to bring a row to ~target_j
   // iterations, no more (idle warps issue nothing, partial ones waste FP64)
   const int best_w = (int)std::min<int64_t>(ntmax / 32, std::max<int64_t>(1, (W + 32 * target_j - 1) / (32 * target_j)));
-  const int NB = 32 * best_w;
-  const int NW = (NB + 63) / 64;
-  int J = (int)((W + NB - 1) / NB);
+  int J = (int)((W + 32 * best_w - 1) / (32 * best_w));
   struct Seg { int item, k, begin, len; bool split; };
   std::vector<Seg> segs;
-  std::vector<int> order, lane, cnt, load;
+  std::vector<int> order, cnt, bwarp, bcol, load;
   std::vector<int> nseg(n, 1);
-  // room[t * NW ...]: bit b set while lane b holds at most t ops
-  std::vector<uint64_t> room;
   while (true) {
     if (maxops > J && J < 2) J = 2;
     segs.clear();
@@ -653,31 +652,26 @@ DProg2 schedule2(const ItemList& items, int ntmax, int target_j, EntryBuf& out, 
     }
     order.resize(segs.size());
     for (int si = 0; si < (int)segs.size(); ++si) order[cnt[segs[si].len]++] = si;
-    room.assign((size_t)J * NW, ~0ull);
-    if (NB & 63)
-      for (int t = 0; t < J; ++t) room[(size_t)t * NW + NW - 1] = (1ull << (NB & 63)) - 1;
-    load.assign(NB, 0);
-    lane.resize(order.size());
+    // bundles of 32 into the warps, first fit (heights do not increase)
+    const int nb = (int)((order.size() + 31) / 32);
+    bwarp.assign(nb, -1);
+    bcol.assign(nb, 0);
+    load.assign(best_w, 0);
     bool ok = true;
-    for (size_t o = 0; o < order.size(); ++o) {
-      const int len = segs[order[o]].len + 1;
-      const int b = first_set(&room[(size_t)(J - len) * NW], NW);
-      if (b < 0) { ok = false; break; }
-      lane[o] = b;
-      const int l0 = load[b], l1 = l0 + len;
-      for (int t = l0; t < std::min(l1, J); ++t) room[(size_t)t * NW + (b >> 6)] &= ~(1ull << (b & 63));
-      load[b] = l1;
+    for (int q = 0; q < nb && ok; ++q) {
+      const int h = segs[order[(size_t)q * 32]].len + 1;
+      int w = 0;
+      while (w < best_w && load[w] + h > J) ++w;
+      if (w == best_w) {
+        ok = false;
+        break;
+      }
+      bwarp[q] = w;
+      bcol[q] = load[w];
+      load[w] += h;
     }
     if (ok) break;
     ++J;
-  }
-  // segments per lane in placement order (CSR)
-  std::vector<int> lane_off(NB + 1, 0), lane_seg(order.size());
-  for (int b : lane) ++lane_off[b + 1];
-  for (int b = 0; b < NB; ++b) lane_off[b + 1] += lane_off[b];
-  {
-    std::vector<int> cur(lane_off.begin(), lane_off.end() - 1);
-    for (size_t o = 0; o < order.size(); ++o) lane_seg[cur[lane[o]]++] = order[o];
   }
   // partial slots of split items, contiguous per item
   std::vector<int> slot0(n, -1);
@@ -686,30 +680,45 @@ DProg2 schedule2(const ItemList& items, int ntmax, int target_j, EntryBuf& out, 
     if (nseg[i] > 1) { slot0[i] = slot_base + nslot; nslot += nseg[i]; }
   if (slot_base + nslot >= 65535) throw Error(WG_ERANGE, "program exceeds 65535 partial slots");
   int used = 0;
-  for (int b = 0; b < NB; ++b) if (lane_off[b + 1] > lane_off[b]) used = b + 1;
-  const int nt = ((used + 31) / 32) * 32;
+  for (int w = 0; w < best_w; ++w) if (load[w] > 0) used = w + 1;
+  const int nt = 32 * used;
   pr.J = J;
   pr.nt = nt;
   pr.nslot = nslot;
-  // every position is written: a lane's segments, then NOPs to J
+  // every position is written: idle lanes and columns get NOPs carrying their
+  // column's kind
   out.resize(out.size() + (size_t)J * nt);
   DEntry* base = out.data() + pr.off;
-  const DEntry nop{pack_code(0, 0, 0, op::NOP), 0.0};
-  for (int t = 0; t < nt; ++t) {
-    int j = 0;
-    for (int x = lane_off[t]; x < lane_off[t + 1]; ++x) {
-      const Seg& sg = segs[lane_seg[x]];
+  std::vector<uint32_t> kind((size_t)J * used, col::NOP);
+  const int nb = (int)bwarp.size();
+  for (int q = 0; q < nb; ++q) {
+    const int w = bwarp[q], h = segs[order[(size_t)q * 32]].len + 1;
+    bool fin = false;
+    for (int l = 0; l < 32 && (size_t)q * 32 + l < order.size(); ++l)
+      fin |= !segs[order[(size_t)q * 32 + l]].split;
+    for (int t = 0; t + 1 < h; ++t) kind[(size_t)(bcol[q] + t) * used + w] = col::PROD;
+    kind[(size_t)(bcol[q] + h - 1) * used + w] = fin ? col::FIN : col::PART;
+  }
+  for (int j = 0; j < J; ++j)
+    for (int t = 0; t < nt; ++t)
+      base[(size_t)j * nt + t] = DEntry{pack_code(0, 0, 0, op::NOP, kind[(size_t)j * used + t / 32]), 0.0};
+  for (int q = 0; q < nb; ++q) {
+    const int w = bwarp[q], h = segs[order[(size_t)q * 32]].len + 1;
+    const int end = bcol[q] + h - 1;  // the bundle's finalize column
+    for (int l = 0; l < 32 && (size_t)q * 32 + l < order.size(); ++l) {
+      const Seg& sg = segs[order[(size_t)q * 32 + l]];
       const Item& it = items.items[sg.item];
       const Ent* e = items.ents.data() + items.off[sg.item] + sg.begin;
-      for (int q = 0; q < sg.len; ++q, ++j)
-        base[(size_t)j * nt + t] = DEntry{pack_code(e[q].a, e[q].b, 0, op::PROD), e[q].p};
+      const int t = 32 * w + l;
+      int j = end - sg.len;
+      for (int x = 0; x < sg.len; ++x, ++j)
+        base[(size_t)j * nt + t] = DEntry{pack_code(e[x].a, e[x].b, 0, op::PROD, col::PROD), e[x].p};
+      const uint32_t k = kind[(size_t)end * used + w];
       if (sg.split)
-        base[(size_t)j * nt + t] = DEntry{pack_code(0, 0, slot0[sg.item] + sg.k, op::FIN_PART), 0.0};
+        base[(size_t)end * nt + t] = DEntry{pack_code(0, 0, slot0[sg.item] + sg.k, op::FIN_PART, k), 0.0};
       else
-        base[(size_t)j * nt + t] = DEntry{pack_code(it.c, it.fa, it.fb, it.fin), 0.0};
-      ++j;
+        base[(size_t)end * nt + t] = DEntry{pack_code(it.c, it.fa, it.fb, it.fin, k), 0.0};
     }
-    for (; j < J; ++j) base[(size_t)j * nt + t] = nop;
   }
   // combine entries (with comb_warp: largest first, the first nbig, those
   // of at least comb_warp partial sums, combined by a warp each); the rest
