@@ -358,6 +358,9 @@ struct PackOptions2 {
   // device memory (L2-resident) instead
   int64_t smem_limit_doubles = 227 * 1024 / 8;
   int target_j = (int)pack_knob("WG_PACK_TARGET_J", 3, 1, 16);  // iterations per row the lane scheduler aims for
+  // iterations per same-row level of a root task the lane scheduler aims for
+  // (levels within one warp synchronize that warp only)
+  int level_j = (int)pack_knob("WG_PACK_LEVEL_J", 3, 1, 32);
   // split clades of the forward programs with at least this many partial
   // sums are combined by a warp each (0: every one by a thread; adjoint
   // programs always combine by thread).  Measured on 5,000 config-1

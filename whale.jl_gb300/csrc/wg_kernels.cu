@@ -580,8 +580,16 @@ template <int NTG, bool REVERSE, unsigned FIN, class OnFin, class Comb>
 __device__ __forceinline__ void chain_levels(const DEntry* __restrict__ E, const DProg2* __restrict__ progs, int nlvl,
                                              int wl, int tix, const double* A, const double* B, double* part,
                                              double ph, double ps, OnFin onfin, Comb comb) {
-  auto sync = [] {
-    if (NTG == 32) __syncwarp();
+  // Threads a level's work occupies: its lanes, its one-thread combines and
+  // its warp combines.  wl and tix are unrotated (lane l is thread l), so a
+  // level within 32 threads is warp 0's alone, and a barrier between two such
+  // levels (or inside one) is that warp's; the other warps pass them and wait
+  // at the next CTA barrier, which every thread reaches in the same order.
+  auto width = [](const DProg2& p) {
+    return max(max(p.nt, p.ncomb - (int)p.nbig), 32 * min((int)p.nbig, NTG / 32));
+  };
+  auto sync = [](bool narrow) {
+    if (NTG == 32 || narrow) __syncwarp();
     else __syncthreads();
   };
   if (nlvl <= 0) return;
@@ -612,11 +620,12 @@ __device__ __forceinline__ void chain_levels(const DEntry* __restrict__ E, const
         lane_step<FIN>(x.kind, x.f0, x.f1, x.f2, x.opc, x.p, A, B, part, ph, ps, onfin, acc);
       }
     }
+    const bool narrow = width(cur) <= 32;
     if (cur.ncomb) {
-      sync();
+      sync(narrow);
       run_comb_reg<NTG, !REVERSE>(E, cur, cr, part, comb, tix);
     }
-    sync();
+    sync(narrow && more && width(nxt) <= 32);  // (the last level ends on a CTA barrier)
     if (more) {
       cur = nxt;
       nxt = nn;
@@ -816,7 +825,7 @@ __device__ __forceinline__ void fwd_task(const KArgs2& A, const DTask& T, int ro
         const double ca = A.params[3 * NR + A.K + 1], cb = A.params[3 * NR + A.K + 2];
         auto lcomb = [&](unsigned, unsigned c, unsigned, unsigned, double acc) { cur[c] = fma(ca, acc, cb * cur[c]); };
         auto lfin = [&](unsigned c, double v, double) { cur[c] = v; };
-        chain_levels<NT, false, op::FIN_LVL>(E, A.progs + T.lvl, T.nlvl, lane, tid, cur, cur, part, cb, ca, lfin,
+        chain_levels<NT, false, op::FIN_LVL>(E, A.progs + T.lvl, T.nlvl, tid, tid, cur, cur, part, cb, ca, lfin,
                                              lcomb);
       }
     }
@@ -1240,7 +1249,7 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
       bar[c] = v;
       Gs[c] = g;
     };
-    chain_levels<NT, true, op::FIN_TLVL>(E, A.progs + T.tlvl, T.nlvl, lane, tid, bar, L0, part, 1.0, ca, tfin,
+    chain_levels<NT, true, op::FIN_TLVL>(E, A.progs + T.tlvl, T.nlvl, tid, tid, bar, L0, part, 1.0, ca, tfin,
                                          tcomb);
     // ∂/∂ca = Σ bar[γ]·Πroot(γ) = ½ Σ_x G[x]·L[x] (each split counted twice)
     for (int c = tid; c < R; c += NT) acc4[0] += 0.5 * Gs[c] * L0[c];

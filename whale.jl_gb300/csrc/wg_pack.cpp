@@ -1040,10 +1040,10 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
         T.nlvl = nl;
         T.lvl = (int64_t)tb.progs.size();
         for (int L = 0; L < nl; ++L)
-          tb.progs.push_back(schedule2(lw[L], NT, opt.target_j, entries, 0, opt.comb_warp));
+          tb.progs.push_back(schedule2(lw[L], NT, opt.level_j, entries, 0, opt.comb_warp));
         if (opt.adjoint) {
           T.tlvl = (int64_t)tb.progs.size();
-          for (int L = 0; L < nl; ++L) tb.progs.push_back(schedule2(tlw[L], NT, opt.target_j, entries));
+          for (int L = 0; L < nl; ++L) tb.progs.push_back(schedule2(tlw[L], NT, opt.level_j, entries));
         }
         for (const DProg2& q : tb.progs) T.rslot = std::max(T.rslot, (int32_t)q.nslot);
       }
@@ -1198,13 +1198,12 @@ Packed2 pack_batch2(const Model& m, const std::vector<const CCD*>& ccds, const P
     if (!c.empty()) std::memcpy(P.entries.data() + entry_off[i], c.data(), c.size() * sizeof(DEntry));
     EntryBuf().swap(c);
   });
-  // heaviest tasks first inside each launch
-  auto by_cost = [&](int a, int b) {
-    const DTask& x = P.tasks[a];
-    const DTask& y = P.tasks[b];
-    return (int64_t)(x.dup.J + x.tdup.J) * m.nrow[x.node] + x.init.J >
-           (int64_t)(y.dup.J + y.tdup.J) * m.nrow[y.node] + y.init.J;
+  // heaviest tasks first inside each launch (a root task's same-row levels
+  // run one after another, each about as long as a row of six entries)
+  auto task_cost = [&](const DTask& x) {
+    return (int64_t)(x.dup.J + x.tdup.J) * m.nrow[x.node] + x.init.J + 6 * (int64_t)x.nlvl;
   };
+  auto by_cost = [&](int a, int b) { return task_cost(P.tasks[a]) > task_cost(P.tasks[b]); };
   for (auto& L : P.levels) std::stable_sort(L.begin(), L.end(), by_cost);
   for (auto& L : P.levels_h) std::stable_sort(L.begin(), L.end(), by_cost);
   for (auto& L : P.levels_g) std::stable_sort(L.begin(), L.end(), by_cost);
