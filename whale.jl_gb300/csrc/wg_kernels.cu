@@ -467,6 +467,30 @@ __device__ __forceinline__ void lane_step(unsigned kind, unsigned f0, unsigned f
   }
 }
 
+// Entries j0..J-1 of a lane's program streamed from memory (e: the lane's
+// entry 0, nt: the program's lanes), four at a time with the next four's
+// loads in flight while the four before them run.
+template <unsigned FIN, class OnFin>
+__device__ __forceinline__ void stream_steps(const ulonglong2* __restrict__ e, int nt, int j0, int J, const double* A,
+                                             const double* B, double* part, double ph, double ps, OnFin& onfin,
+                                             double& acc) {
+  const ulonglong2 nop = make_ulonglong2(0, 0);  // column kind NOP: no work
+  ulonglong2 c[4], nx[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) c[u] = j0 + u < J ? __ldg(e + (size_t)(j0 + u) * nt) : nop;
+  for (int j = j0; j < J; j += 4) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) nx[u] = j + 4 + u < J ? __ldg(e + (size_t)(j + 4 + u) * nt) : nop;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const Raw x = decode(c[u]);
+      lane_step<FIN>(x.kind, x.f0, x.f1, x.f2, x.opc, x.p, A, B, part, ph, ps, onfin, acc);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) c[u] = nx[u];
+  }
+}
+
 // Row program of the branch recursion streamed from memory (programs deeper
 // than the register-resident instantiations): entries as in lane_step.
 //   PROD:    acc = fma(p·cur[a], cur[b], acc)
@@ -481,10 +505,7 @@ __device__ __forceinline__ void run_rows(const DEntry* __restrict__ E, const DPr
     if (STORE) tab[c] = v;
   };
   double acc = 0.0;
-  for (int j = 0; j < pr.J; ++j, e += pr.nt) {
-    const Raw x = decode(__ldg(e));
-    lane_step<op::FIN_DUP>(x.kind, x.f0, x.f1, x.f2, x.opc, x.p, cur, cur, part, ph, ps, onfin, acc);
-  }
+  stream_steps<op::FIN_DUP>(e, pr.nt, 0, pr.J, cur, cur, part, ph, ps, onfin, acc);
 }
 
 // A lane's share of a row program held in registers for all rows of a node:
@@ -614,6 +635,8 @@ __device__ __forceinline__ void chain_levels(const DEntry* __restrict__ E, const
     if (wl < cur.nt) {
       double acc = 0.0;
       raw_steps<kLvlJ, FIN>(lp, A, B, part, ph, ps, onfin, acc);
+      // (one entry at a time past the registers: the root kernels' register
+      // budget has no room for a streaming window)
       const ulonglong2* e = reinterpret_cast<const ulonglong2*>(E + cur.off) + wl;
       for (int j = kLvlJ; j < cur.J; ++j) {
         const Raw x = decode(__ldg(e + (size_t)j * cur.nt));
@@ -1061,10 +1084,7 @@ __device__ __forceinline__ void adj_rows(const DEntry* __restrict__ E, const DTa
         bn[c] = v;
         if constexpr (!ONEDOT) Gs[c] = g;
       };
-      for (int j = 0; j < td.J; ++j, e += td.nt) {
-        const Raw x = decode(__ldg(e));
-        lane_step<op::FIN_ADJ>(x.kind, x.f0, x.f1, x.f2, x.opc, x.p, bb, Lp, part, ph, ps, onfin, acc);
-      }
+      stream_steps<op::FIN_ADJ>(e, td.nt, 0, td.J, bb, Lp, part, ph, ps, onfin, acc);
     }
     if (td.ncomb) {
       __syncthreads();
