@@ -19,6 +19,10 @@ The packer's knobs decide how a batch maps onto the GPU:
   adj_overlap 2: each size class's adjoint follows its own forward at the
               class's stream priority; 1 (3): at the lowest (highest)
               priority; 0: after every class's forward (WG_ADJ_OVERLAP)
+  level_j     iterations per same-row level a root task's level programs
+              aim for (levels within one warp synchronize that warp only)
+  comb_warp   forward split clades of at least this many partial sums are
+              combined by a warp each (0: by one thread each)
 
 ``tune(wm, ccds)`` builds the batch under candidate settings, times a few
 evaluations of each on the device (CUDA events around the launch sequence,
@@ -30,8 +34,8 @@ for evaluations.  Every setting gives the same log-likelihood and gradient
 to rounding; only the layout and the time change.
 
 The knobs reach the packer through environment variables (WG_PACK_TARGET_OPS,
-WG_PACK_TARGET_J, WG_PACK_ROOT_GROUP, WG_PACK_HEAVY_OPS), set only while a
-candidate batch is built.
+WG_PACK_TARGET_J, WG_PACK_ROOT_GROUP, WG_PACK_HEAVY_OPS, WG_PACK_LEVEL_J,
+WG_PACK_COMB_WARP, ...), set only while a candidate batch is built.
 """
 from __future__ import annotations
 
@@ -58,7 +62,8 @@ N_CLASSES = max(len(b) for b in CLASS_BOUNDS) + 1
 
 DEFAULTS: Dict[str, int] = {"target_ops": 480, "target_j": 3, "root_group": 16, "heavy_ops": 1024,
                             **{f"heavy_c{i}": 0 for i in range(N_CLASSES)},
-                            "classes": 0, "persistent": 0, "persist_ctas": 3, "adj_overlap": 2}
+                            "classes": 0, "persistent": 0, "persist_ctas": 3, "adj_overlap": 2, "level_j": 3,
+                            "comb_warp": 24}
 NEIGHBOURS: Dict[str, Tuple[int, ...]] = {
     "target_ops": (240, 320, 480, 720, 960),
     "target_j": (2, 3, 4, 5),
@@ -68,11 +73,13 @@ NEIGHBOURS: Dict[str, Tuple[int, ...]] = {
     "classes": tuple(range(len(CLASS_BOUNDS))),
     "persistent": (0, 1),
     "adj_overlap": (0, 1, 2, 3),
+    "level_j": (2, 3, 4),
+    "comb_warp": (0, 16, 24, 48),
 }
 _ENV = {"target_ops": "WG_PACK_TARGET_OPS", "target_j": "WG_PACK_TARGET_J", "root_group": "WG_PACK_ROOT_GROUP",
         "heavy_ops": "WG_PACK_HEAVY_OPS", **{f"heavy_c{i}": f"WG_PACK_HEAVY_OPS_C{i}" for i in range(N_CLASSES)},
         "classes": "WG_CLASS_BOUNDS", "persistent": None, "persist_ctas": "WG_PERSIST_CTAS",
-        "adj_overlap": "WG_ADJ_OVERLAP"}
+        "adj_overlap": "WG_ADJ_OVERLAP", "level_j": "WG_PACK_LEVEL_J", "comb_warp": "WG_PACK_COMB_WARP"}
 
 
 def _env_value(knob: str, v: int):
