@@ -509,8 +509,9 @@ __device__ __forceinline__ void run_rows(const DEntry* __restrict__ E, const DPr
 }
 
 // A lane's share of a row program held in registers for all rows of a node:
-// (f0 | f1 << 16, f2 | op << 16, p) per iteration.  Rows then issue no entry
-// loads; operand loads of every iteration are known up front.
+// (f0 | f1 << 16, f2 | op << 16 | column kind << 24, p) per iteration.  Rows
+// then issue no entry loads; operand loads of every iteration are known up
+// front.
 template <int MAXJ>
 struct LaneProg {
   uint32_t ab[MAXJ];
