@@ -314,7 +314,8 @@ def run_tune(args, W):
     wm, ccds = wl.model, wl.ccds()
     nb = {"classes": tuple(range(len(autotune.CLASS_BOUNDS))), "persistent": (0, 1), "adj_overlap": (0, 1, 2, 3),
           **{f"heavy_c{i}": (0, 512, 2048, 1 << 20) for i in range(autotune.N_CLASSES)},
-          "target_ops": (320, 480, 720), "target_j": (2, 3, 4), "root_group": (8, 16, 32)}
+          "target_ops": (320, 480, 720), "target_j": (2, 3, 4), "root_group": (8, 16, 32), "level_j": (2, 3, 4),
+          "comb_warp": (0, 24, 48)}
     best, b, log = W.tune(wm, ccds, steps=max(3, args.steps), warmup=3, neighbours=nb, rounds=2)
     rep = autotune.report(best, log)
     rep.update({"metric": "autotuned ms per gradient evaluation", "config": {"workload": workload(len(ccds),
