@@ -146,7 +146,8 @@ constexpr uint64_t kValid = 1;     // entry flags (bits 48..63 of code)
 constexpr uint64_t kEnd = 2;
 
 struct alignas(16) DEntry {
-  uint64_t code;  // a | b << 16 | dst << 32 | flags << 48
+  uint64_t code;  // plain programs: a | b << 16 | dst << 32 | flags << 48; batched programs:
+                  // f0 | f1 << 16 | f2 << 32 | op << 48 | column kind << 56
   double p;
 };
 

@@ -720,6 +720,16 @@ DProg2 schedule2(const ItemList& items, int ntmax, int target_j, EntryBuf& out, 
         base[(size_t)end * nt + t] = DEntry{pack_code(it.c, it.fa, it.fb, it.fin, k), 0.0};
     }
   }
+  // every entry fits its column's kind (the kernels take one branch per warp
+  // and column; a product in a finalize column would be skipped)
+  for (size_t x = 0; x < (size_t)J * nt; ++x) {
+    const uint64_t code = base[x].code;
+    const uint32_t o = (uint32_t)((code >> 48) & 0xFFu), kd = (uint32_t)(code >> 56);
+    const bool fits = o == op::NOP || (kd == col::PROD ? o == op::PROD
+                                                        : kd == col::FIN ? o != op::PROD
+                                                                         : kd == col::PART && o == op::FIN_PART);
+    if (!fits) throw Error(WG_ESTATE, "internal: program entry does not fit its column");
+  }
   // combine entries (with comb_warp: largest first, the first nbig, those
   // of at least comb_warp partial sums, combined by a warp each); the rest
   // are combined by a thread each
