@@ -585,12 +585,6 @@ inline double bits_to_double(uint64_t b) {
   return d;
 }
 
-inline int first_set(const uint64_t* w, int nw) {
-  for (int i = 0; i < nw; ++i)
-    if (w[i]) return 64 * i + __builtin_ctzll(w[i]);
-  return -1;
-}
-
 // Lane programs with fused finalize.  An item (one clade) is its products
 // followed by its finalize op; items longer than J ops are split into
 // segments ending in FIN_PART, finished by a combine entry after a barrier.
