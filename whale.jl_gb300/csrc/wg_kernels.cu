@@ -1222,7 +1222,7 @@ __device__ __forceinline__ void adj_task(const KArgs2& A, const DTask& T, int ro
   const int n = mn.w;
   double* bar = sm;
   double* barn = sm + W2;
-  double* L0 = sm + 2 * W2;  // L0, L1 and a third buffer: table rows of the branch
+  double* L0 = sm + 2 * W2;  // L0, L1, a third and (one-dot form) G's row: table rows of the branch
   double* L1 = sm + 3 * W2;
   double* Gs = sm + 5 * W2;
   double* part = sm + 6 * W2;
