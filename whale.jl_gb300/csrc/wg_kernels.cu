@@ -1516,9 +1516,11 @@ __device__ __forceinline__ void publish(const PArgs& P, int task) {
 
 // Persistent forward: any task of the layout (root or branch, rows in shared
 // or device memory) with kNT2L threads; the dynamic shared memory is the
-// largest of the layout's shared-memory tasks.
+// largest of the layout's shared-memory tasks.  Bounded for three CTAs per
+// SM (the default WG_PERSIST_CTAS): the four variants held at once fit ~165
+// registers without spills; the grid follows the occupancy it compiles to.
 template <bool TABLES>
-__global__ void __launch_bounds__(kNT2L, 4) k_fwd_persist(const KArgs2 A, const PArgs P) {
+__global__ void __launch_bounds__(kNT2L, 3) k_fwd_persist(const KArgs2 A, const PArgs P) {
   extern __shared__ __align__(128) double smem_dyn[];
   __shared__ int s_t;
   for (;;) {
@@ -1540,7 +1542,7 @@ __global__ void __launch_bounds__(kNT2L, 4) k_fwd_persist(const KArgs2 A, const 
 }
 
 // Persistent adjoint, tickets from the root level down.
-__global__ void __launch_bounds__(kNT2L, 4) k_adj_persist(const KArgs2 A, const PArgs P) {
+__global__ void __launch_bounds__(kNT2L, 3) k_adj_persist(const KArgs2 A, const PArgs P) {
   extern __shared__ __align__(128) double smem_dyn[];
   __shared__ int s_t;
   for (;;) {
