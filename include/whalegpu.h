@@ -159,7 +159,10 @@ int wg_ccd_export(const wg_ccd* c, int32_t* nleaves, int64_t* counts, int32_t* s
 /* ---- device-resident batch of families --------------------------------
  * The batch keeps pointers to its CCDs (wg_logpdf_plain and wg_track_device
  * build their own layouts from them on first use): destroy the batch before
- * its CCDs. */
+ * its CCDs.  Limits (WG_ERANGE beyond them): a family's clades compatible
+ * with one species node below 32,768 and a CCD below 65,535 clades (16-bit
+ * program fields; the reference has no such limit), a program's partial sums
+ * below 65,535. */
 int wg_batch_create(wg_ctx* ctx, const wg_model* m, wg_ccd* const* ccds, int32_t n_ccds, uint32_t flags,
                     wg_batch** out);
 int wg_batch_destroy(wg_batch* b);
